@@ -1,0 +1,451 @@
+#!/usr/bin/env python
+"""bench.py — particle-iterations/s of the XPBD cloth solver on synthetic cloth grids.
+
+One step = one frame (frame_dt = 1/60 s) of every cloth of the workload: substeps x
+iterations Jacobi sweeps plus collision, hashing and normals, exactly the work
+VtClothSolverGPU::Simulate does per fixed frame.  particle-iterations per step =
+sum over cloths of N * substeps * iterations.
+
+Default workload: the mixed-size batch (512 independent grid cloths, side log-uniform in
+[16, 256], ~6 M particles, 5 substeps x 10 iterations, sphere + plane each, two pinned
+corners).  Its working set (~3 GB) is far larger than L2, so no flush is needed between
+steps.
+
+Arms:
+  --impl ours (default)  the CUDA solver through the C ABI.  `value`: device-resident
+                         frames timed with CUDA events; `e2e`: the same frames with the
+                         per-frame collider upload from host memory and the positions +
+                         normals read back into pinned host memory inside the timed region.
+                         The JSON line also carries the plain (one cloth at a time)
+                         drop-in solver's rate and p50/p99 frame latency, the dominant
+                         kernel's roofline, and the CPU oracle timed on a bounded sample.
+  --impl reference       the CPU restatement of the reference solver (the oracle; the
+                         reference's own sources cannot be built on these machines),
+                         all host cores, one process per core, bounded sample.
+Multi-GPU (torchrun): each rank runs its own copy of the workload (cloths are
+independent; no collective on the data path) -> weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-iterations/s and p99 frame latency, batched vs plain, same GB300"
+UNIT = "particle-iterations/s"
+
+
+# ---------------------------------------------------------------------------- helpers
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def workload(name: str, seed: int = 0):
+    from velvet_gb300 import workloads as W
+
+    if name == "batched":
+        return W.batched(512, seed=seed)
+    if name == "small":
+        return W.small()
+    if name == "large":
+        return W.large()
+    if name == "stress":
+        return W.stress(seed=seed)
+    if name == "grid1024":
+        wl = W.stress(seed=seed)
+        spec = wl.cloths[0]
+        spec.attached = [0, spec.side - 1]
+        wl.name = "grid_1024x1024_two_corners"
+        return wl
+    raise SystemExit(f"unknown workload {name}")
+
+
+def pits_per_frame(wl) -> int:
+    return sum(c.num_particles for c in wl.cloths) * wl.substeps * wl.iterations
+
+
+def iteration_bytes(wl) -> float:
+    """Algorithmic bytes of one Jacobi iteration over every cloth:
+    12*C_s + 20*C_b + 12*C_a + 28*N (constraint streams at information size, predicted
+    position read 12 B + inverse mass 4 B + write 12 B per particle)."""
+    b = 0.0
+    for c in wl.cloths:
+        V = c.side
+        Cs = 2 * V * (V - 1) + 2 * (V - 1) ** 2
+        Cb = (V - 1) ** 2
+        Ca = len(c.attached) * V * V
+        b += 12 * Cs + 20 * Cb + 12 * Ca + 28 * V * V
+    return b
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int = 0, pci_bus_id: str | None = None):
+        self.rows: list[list[str]] = []
+        sel = ["-i", pci_bus_id] if pci_bus_id else ["-i", str(device_index)]
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", *sel], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if len(r) >= 8 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 8 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 8 for k in range(4)
+                          if r[4 + k].lower() == "active"})
+        pw = [float(r[2]) for r in self.rows if len(r) >= 8 and r[2].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm), "power_w_max": max(pw) if pw else None}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------- oracle legs
+def _oracle_worker(args):
+    """Runs `frames` frames of the given cloths on the CPU oracle; returns (pits, seconds)."""
+    idx, wl_name, seed, frames = args
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle import Oracle
+    from velvet_gb300 import workloads as W
+
+    wl = workload(wl_name, seed)
+    pits, secs = 0, 0.0
+    for i in idx:
+        spec = wl.cloths[i]
+        o = Oracle()
+        W.build_plain(spec, o)
+        d = spec.particle_diameter()
+        t0 = time.perf_counter()
+        for f in range(frames):
+            o.update_colliders(spec.colliders(f))
+            o.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin, d)
+        secs += time.perf_counter() - t0
+        pits += spec.num_particles * wl.substeps * wl.iterations * frames
+        o.close()
+    return pits, secs
+
+
+def sample_indices(wl, budget_particles: int) -> list[int]:
+    """Every k-th cloth, preserving the size distribution, up to ~budget particles."""
+    n = len(wl.cloths)
+    total = sum(c.num_particles for c in wl.cloths)
+    k = max(1, int(math.ceil(total / max(1, budget_particles))))
+    return list(range(0, n, k))
+
+
+def cpu_baseline_single(wl_name: str, seed: int, budget_s: float = 15.0) -> dict:
+    """The oracle on one core over a bounded sample of the workload."""
+    wl = workload(wl_name, seed)
+    idx = sample_indices(wl, 250_000)
+    pits, secs = _oracle_worker((idx, wl_name, seed, 1))
+    frames = max(1, min(4, int(budget_s / max(secs, 1e-3))))
+    if frames > 1:
+        p2, s2 = _oracle_worker((idx, wl_name, seed, frames))
+        pits, secs = p2, s2
+    return {"value": pits / secs, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{len(idx)} of {len(wl.cloths)} cloths (every {len(wl.cloths) // max(1, len(idx))}th), "
+                      f"{frames} frame(s), {pits / 1e6:.1f} M particle-iterations in {secs:.1f} s"}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle
+
+    oracle.lib()  # build once here, before the workers load it
+    wl = workload(args.workload, args.seed)
+    cores = os.cpu_count() or 1
+    idx = sample_indices(wl, 400_000 * max(1, cores // 4))
+    chunks = [idx[k::cores] for k in range(cores)]
+    chunks = [c for c in chunks if c]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(chunks)) as pool:
+        step_times, step_pits = [], []
+        for s in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_worker, [(c, args.workload, args.seed, 1) for c in chunks])
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                step_times.append(dt)
+                step_pits.append(sum(r[0] for r in res))
+    value = sum(step_pits) / sum(step_times)
+    sample = (f"{len(idx)} of {len(wl.cloths)} cloths (size distribution kept), one frame per step "
+              f"on {len(chunks)} processes")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * statistics.mean(step_times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic grid cloths (seeded), CPU restatement of the reference GPU solver",
+        "config": {"workload": wl.name, "cloths_sampled": len(idx), "substeps": wl.substeps,
+                   "iterations": wl.iterations},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(chunks), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------- GPU arm
+def build_plain_solvers(wl):
+    import velvet_gb300 as vg
+    from velvet_gb300 import workloads as W
+
+    solvers = []
+    for spec in wl.cloths:
+        s = vg.ClothSolver()
+        W.build_plain(spec, s)
+        solvers.append((s, spec, spec.particle_diameter()))
+    return solvers
+
+
+def plain_frame(wl, solvers, frame, stream, upload_colliders):
+    for s, spec, d in solvers:
+        if upload_colliders:
+            s.update_colliders(spec.colliders(frame))
+        s.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                   wl.collision_margin, d, stream)
+
+
+def launch_total(solvers) -> int:
+    import ctypes as C
+
+    import velvet_gb300 as vg
+
+    tot = 0
+    for s, _, _ in solvers:
+        v = C.c_uint64()
+        vg._abi.check(vg.lib().vt_solver_launch_count(s.handle, C.byref(v)), "vt_solver_launch_count")
+        tot += v.value
+    return tot
+
+
+def profile_frames(args) -> None:
+    """Builds the workload and runs `--profile-frames` frames on the default stream:
+    the command ncu captures (nothing else launches kernels)."""
+    import torch
+
+    wl = workload(args.workload, args.seed)
+    solvers = build_plain_solvers(wl)
+    for f in range(args.profile_frames):
+        plain_frame(wl, solvers, f, None, upload_colliders=False)
+    torch.cuda.synchronize()
+    for s, _, _ in solvers:
+        s.sync()
+    print(json.dumps({"profiled_frames": args.profile_frames, "workload": wl.name,
+                      "particles": wl.num_particles}))
+
+
+def timed_device(step_fn, steps, warmup, stream, dist_sync):
+    import torch
+
+    for f in range(warmup):
+        step_fn(f)
+    torch.cuda.synchronize()
+    dist_sync()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for k in range(steps):
+        step_fn(warmup + k)
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    dist_sync()
+    per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    return ev[0].elapsed_time(ev[steps]), per
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="batched")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="only run this many frames of the workload and exit (for ncu captures)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    if args.profile_frames:
+        profile_frames(args)
+        return
+
+    import torch
+
+    import velvet_gb300 as vg
+    from velvet_gb300 import _abi
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def dist_sync():
+        if dist is not None:
+            dist.barrier()
+
+    wl = workload(args.workload, args.seed)
+    stream = torch.cuda.Stream()
+    pits = pits_per_frame(wl)
+
+    # ---- plain drop-in solver, one cloth at a time (the current headline form)
+    solvers = build_plain_solvers(wl)
+    step = lambda f: plain_frame(wl, solvers, f, stream, upload_colliders=False)  # noqa: E731
+    props = torch.cuda.get_device_properties(local)
+    bus = getattr(props, "pci_bus_id", None)
+    pci = None
+    if bus is not None:
+        pci = f"{getattr(props, 'pci_domain_id', 0):08x}:{bus:02x}:{getattr(props, 'pci_device_id', 0):02x}.0"
+    launches0 = launch_total(solvers)
+    clocks = ClockSampler(local, pci)
+    total_ms, per = timed_device(step, args.steps, args.warmup, stream, dist_sync)
+    clock_info = clocks.stop()
+    launches = launch_total(solvers) - launches0
+    # launches counted cover warm-up too; keep only the timed steps' share
+    launches_timed = int(round(launches * args.steps / (args.steps + args.warmup)))
+
+    elapsed = torch.tensor([total_ms], device="cuda")
+    if dist is not None:
+        dist.all_reduce(elapsed, op=dist.ReduceOp.MAX)
+    total_ms = float(elapsed.item())
+    value = pits * args.steps * world / (total_ms / 1000.0)
+
+    # ---- roofline of the dominant stage: one Jacobi iteration (bend + solve)
+    _abi.profiler_reset()
+    _abi.profiler_enable(True)
+    for k in range(2):
+        step(args.warmup + args.steps + k)
+    torch.cuda.synchronize()
+    prof = _abi.profiler_read()
+    _abi.profiler_enable(False)
+    it_launch = prof.get("solve", (0, 0.0))
+    bend = prof.get("bend", (0, 0.0))
+    roofline = None
+    peak, peak_kind = measured_peak_hbm()
+    if it_launch[0]:
+        iters = 2 * wl.substeps * wl.iterations  # per-cloth iterations in the profiled frames
+        t_iter_ms = (it_launch[1] + bend[1]) / iters  # summed over cloths
+        ach = iteration_bytes(wl) / (t_iter_ms / 1000.0) / 1e9
+        roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                    "traffic": None, "kernel": "bend+solve (one Jacobi iteration, all cloths)",
+                    "peak_source": f"{peak_kind} hbm_gbs",
+                    "stage_ms_per_frame": {k: v[1] / 2 for k, v in prof.items()}}
+
+    # ---- end to end through the C ABI with host buffers
+    n_tot = wl.num_particles
+    host_pos = torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True)
+    host_nrm = torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True)
+    offs = np.cumsum([0] + [c.num_particles for c in wl.cloths])
+
+    def e2e_step(f):
+        plain_frame(wl, solvers, f, stream, upload_colliders=True)
+        for i, (s, spec, _) in enumerate(solvers):
+            n = spec.num_particles
+            p = host_pos.data_ptr() + 12 * int(offs[i])
+            q = host_nrm.data_ptr() + 12 * int(offs[i])
+            _abi.check(vg.lib().vt_positions_get(s.handle, 0, n, p, 1, vg.stream_handle(stream)), "positions")
+            _abi.check(vg.lib().vt_normals_get(s.handle, 0, n, q, 1, vg.stream_handle(stream)), "normals")
+        stream.synchronize()
+
+    for f in range(args.warmup):
+        e2e_step(f)
+    dist_sync()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for k in range(e2e_steps):
+        e2e_step(k)
+    e2e_s = time.perf_counter() - t0
+    e2e_t = torch.tensor([e2e_s], device="cuda")
+    if dist is not None:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = pits * e2e_steps * world / float(e2e_t.item())
+    h2d = len(wl.cloths) * (2 * 208 + 128)  # colliders + domain parameter block per cloth
+    d2h = n_tot * 24
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_single(args.workload, args.seed)
+
+    if rank == 0:
+        per_sorted = sorted(per)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic grid cloths generated from the config (seeded), no dataset",
+            "config": {"workload": wl.name, "form": "plain (one cloth at a time)",
+                       "cloths_per_gpu": len(wl.cloths), "particles_per_gpu": n_tot,
+                       "substeps": wl.substeps, "iterations": wl.iterations,
+                       "l2": "inputs larger than L2 (working set ~%.1f GB)" % (n_tot * 500 / 1e9),
+                       "parallelism": f"independent cloths per GPU x {world}"},
+            "p50_frame_ms": statistics.median(per), "p99_frame_ms": per_sorted[min(len(per) - 1, int(0.99 * len(per)))],
+            "clocks": clock_info,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_timed,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

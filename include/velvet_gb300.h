@@ -1,0 +1,335 @@
+/*
+ * velvet_gb300.h — C ABI of the GB300 XPBD cloth solver.
+ *
+ * The surface follows the GPU cloth solver of Velvet (vitalight/Velvet):
+ *   - the class API of VtClothSolverGPU (Velvet/VtClothSolverGPU.hpp:114-205):
+ *     AddCloth / AddStretch / AddAttachSlot / AddAttach / AddBend /
+ *     UpdateColliders / Simulate, plus the public buffers callers mutate
+ *     (positions, normals, invMasses, attachSlotPositions);
+ *   - the constraint builder VtClothObjectGPU::Start (Velvet/VtClothObjectGPU.hpp:43-147);
+ *   - the spatial-hash launch function HashObjects (Velvet/SpatialHashGPU.cuh:17-24).
+ *
+ * Conventions (differences from the reference are deliberate and listed):
+ *   - every entry point returns a vt_status; nothing calls exit() (the reference's
+ *     checkCudaErrors does) and no C++ exception crosses the ABI;
+ *   - vector data crosses the ABI as float triples (x, y, z), the memory layout of
+ *     glm::vec3 arrays; matrices are 16 floats, column-major (glm::mat4 layout);
+ *   - `stream` arguments are cudaStream_t passed as void* (NULL = legacy default
+ *     stream); work is enqueued asynchronously, getters that write host memory
+ *     synchronise the stream first;
+ *   - one handle must not be used from two host threads at once; separate handles
+ *     are independent (the reference keeps its parameters in a process-wide
+ *     __constant__ block and a global singleton, so it is not re-entrant at all).
+ *
+ * Arithmetic is FP32 with IEEE division and square root and no fused multiply-add,
+ * and every Jacobi sum is accumulated per particle in constraint order, so results do
+ * not depend on thread scheduling: two runs on the same inputs give identical bits.
+ */
+#ifndef VELVET_GB300_H
+#define VELVET_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VT_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ status codes */
+typedef int32_t vt_status;
+#define VT_OK                    0
+#define VT_ERR_INVALID_ARGUMENT (-1)  /* null pointer, index out of range, bad size  */
+#define VT_ERR_OUT_OF_MEMORY    (-2)  /* device or host allocation failed           */
+#define VT_ERR_CUDA             (-3)  /* a CUDA runtime call failed (see vt_last_error) */
+#define VT_ERR_NOT_FOUND        (-4)  /* unknown request / cloth id                  */
+#define VT_ERR_STATE            (-5)  /* call not valid in the handle's current state */
+#define VT_ERR_CAPACITY         (-6)  /* a fixed limit or budget would be exceeded    */
+#define VT_ERR_NUMERIC          (-7)  /* a device-side check found NaN/Inf state      */
+#define VT_ERR_TIMEOUT          (-8)  /* a bounded wait gave up                       */
+
+/* Collider kinds, in the order of Velvet's ColliderType (Velvet/Common.hpp:67-72). */
+#define VT_COLLIDER_SPHERE 0
+#define VT_COLLIDER_PLANE  1
+#define VT_COLLIDER_CUBE   2
+
+/* Simulation parameters: VtSimParams (Velvet/Common.hpp:19-48), same fields, same
+ * defaults (vt_params_default).  Fields marked "runtime" are maintained by the solver
+ * (AddCloth writes them, Velvet/VtClothSolverGPU.hpp:122-125). */
+typedef struct vt_params {
+    int32_t  num_substeps;             /* 2                                        */
+    int32_t  num_iterations;           /* 4                                        */
+    int32_t  max_num_neighbors;        /* 64 (1..64)                               */
+    float    max_speed;                /* 50; AddCloth sets 2*d/dt*substeps        */
+    float    gravity[3];               /* (0, -9.8, 0)                             */
+    float    bend_compliance;          /* 0                                        */
+    float    damping;                  /* 0.25                                     */
+    float    relaxation_factor;        /* 1                                        */
+    float    long_range_stretchiness;  /* 1.2                                      */
+    float    collision_margin;         /* 0.06                                     */
+    float    friction;                 /* 0.1                                      */
+    int32_t  enable_self_collision;    /* 1                                        */
+    int32_t  interleaved_hash;         /* 3: hash every n-th substep               */
+    uint32_t num_particles;            /* runtime                                  */
+    float    particle_diameter;        /* runtime: the last cloth's diameter       */
+    float    delta_time;               /* fixed frame time, 1/60                   */
+    float    particle_diameter_scalar; /* 1.5                                      */
+    float    hash_cell_size_scalar;    /* 1.5                                      */
+} vt_params;
+
+/* One SDF collider: SDFCollider (Velvet/VtClothSolverGPU.cuh:8-18).  The caller fills
+ * it the way VtClothSolverGPU::UpdateColliders does (Velvet/VtClothSolverGPU.hpp:187-205):
+ * cur_transform is the upper-left 3x3 of the current model matrix, inv_cur_transform
+ * its 4x4 inverse, last_transform the previous frame's model matrix, delta_time the
+ * fixed frame time.  Planes use position.y, spheres position and scale.x (radius),
+ * cubes the matrices and scale. */
+typedef struct vt_sdf_collider {
+    int32_t type;                  /* VT_COLLIDER_*                   */
+    float   position[3];
+    float   scale[3];
+    float   delta_time;
+    float   cur_transform[9];      /* mat3, column-major              */
+    float   inv_cur_transform[16]; /* mat4, column-major              */
+    float   last_transform[16];    /* mat4, column-major              */
+} vt_sdf_collider;
+
+/* Parameters of one spatial-hash build: HashParams (Velvet/SpatialHashGPU.cuh:7-15). */
+typedef struct vt_hash_params {
+    uint32_t num_objects;
+    uint32_t max_num_neighbors;
+    float    cell_spacing;
+    float    cell_spacing2;
+    int32_t  table_size;
+    float    particle_diameter2;
+} vt_hash_params;
+
+typedef struct vt_solver vt_solver;
+
+/* ------------------------------------------------------------------ library */
+
+/* Fills *p with VtSimParams' defaults (Velvet/Common.hpp:21-46). */
+void vt_params_default(vt_params* p);
+
+/* Human-readable name of a status code. */
+const char* vt_status_string(vt_status s);
+
+/* Message of the last failure on the calling host thread ("" if none). */
+const char* vt_last_error(void);
+
+/* ABI version of the loaded library (VT_ABI_VERSION it was built with). */
+int32_t vt_abi_version(void);
+
+/* ------------------------------------------------------------------ plain solver */
+
+/* Creates an empty solver; replaces `new VtClothSolverGPU` + Start()
+ * (Velvet/VtClothSolverGPU.hpp:27-33).  params may be NULL (defaults). */
+vt_status vt_solver_create(const vt_params* params, vt_solver** out);
+
+/* Frees every device and host buffer of the solver (OnDestroy, :50-54). */
+vt_status vt_solver_destroy(vt_solver* s);
+
+/* Reads / replaces the solver's parameter block (Global::simParams). */
+vt_status vt_solver_get_params(const vt_solver* s, vt_params* out);
+vt_status vt_solver_set_params(vt_solver* s, const vt_params* p);
+
+/* AddCloth (Velvet/VtClothSolverGPU.hpp:114-156): appends num_vertices particles at
+ * model * (x, y, z, 1), the triangle indices offset by the previous particle count,
+ * zero velocity, inverse mass 1; sets particle_diameter and max_speed in the params,
+ * resizes the hash table to twice the particle count and snapshots the current
+ * positions as the initial positions of the self-collision filter.
+ * *out_offset receives the index of the cloth's first particle. */
+vt_status vt_cloth_add(vt_solver* s, const float* xyz, uint32_t num_vertices,
+                       const uint32_t* indices, uint32_t num_indices,
+                       const float model[16], float particle_diameter,
+                       int32_t* out_offset);
+
+/* AddStretch (:158-163), in bulk: pairs[2*k], pairs[2*k+1], rest[k]. */
+vt_status vt_stretch_add(vt_solver* s, const int32_t* pairs, const float* rest,
+                         uint32_t count);
+
+/* AddAttachSlot (:165-168): appends a slot; *out_slot gets its index (may be NULL). */
+vt_status vt_attach_slot_add(vt_solver* s, const float xyz[3], int32_t* out_slot);
+
+/* AddAttach (:170-176), in bulk: particle, slot, rest distance.  A distance of exactly
+ * 0 sets that particle's inverse mass to 0, as the reference does. */
+vt_status vt_attach_add(vt_solver* s, const int32_t* particles, const int32_t* slots,
+                        const float* distances, uint32_t count);
+
+/* Long-range attachments in compact form: the constraint set VtClothObjectGPU::
+ * GenerateAttach (Velvet/VtClothObjectGPU.hpp:134-147) appends, i.e. for each slot k in
+ * [first_slot, first_slot + num_slots), in that order, one attachment of every particle
+ * in [particle_begin, particle_begin + particle_count) with rest distance
+ * |slot_k - x_i| taken from the slot position at this call and the particles' current
+ * positions.  The distances are recomputed on the device instead of stored (S x N of
+ * them), with the same FP32 arithmetic, so the results equal those of the expanded
+ * list; inverse masses of particles at distance 0 are set to 0. */
+vt_status vt_attach_generate_lra(vt_solver* s, int32_t first_slot, uint32_t num_slots,
+                                 int32_t particle_begin, uint32_t particle_count);
+
+/* AddBend (:178-185), in bulk: quads[4*k .. 4*k+3], rest_angles[k]. */
+vt_status vt_bend_add(vt_solver* s, const uint32_t* quads, const float* rest_angles,
+                      uint32_t count);
+
+/* VtClothObjectGPU::Start's constraint generation (Velvet/VtClothObjectGPU.hpp:43-58,
+ * 75-147) for a (resolution+1)^2 grid cloth registered at `offset` with the triangle
+ * order of Scene::GenerateClothMesh (Velvet/Scene.hpp:131-168): stretch constraints on
+ * grid edges and both diagonals with rest lengths from the current positions, one
+ * attach slot per entry of `attached` (cloth-local vertex indices) with long-range
+ * attachments of every particle of the cloth, and one bend constraint per quad with
+ * rest angle 0.  Slots get solver-global indices (the reference reuses 0..n-1 for each
+ * cloth, which points a second cloth at the first cloth's slots; not reproduced). */
+vt_status vt_cloth_build_grid_constraints(vt_solver* s, int32_t offset, int32_t resolution,
+                                          const int32_t* attached, uint32_t num_attached);
+
+/* UpdateColliders (:187-205): replaces the collider list (applied in list order). */
+vt_status vt_colliders_set(vt_solver* s, const vt_sdf_collider* colliders, uint32_t count);
+
+/* Simulate (:56-111) for one frame of length frame_dt, after setting substeps,
+ * iterations, relaxation factor, friction, collision margin and particle diameter in
+ * the parameter block (the reference reads them from Global::simParams).  Enqueued on
+ * `stream`; returns without waiting.  Normals are recomputed at the end of the frame. */
+vt_status vt_simulate(vt_solver* s, float frame_dt, int32_t substeps, int32_t iterations,
+                      float relaxation, float friction, float collision_margin,
+                      float particle_diameter, void* stream);
+
+/* Blocks until all work enqueued on the solver has finished; reports a device-side
+ * numeric fault (VT_ERR_NUMERIC) if one was flagged. */
+vt_status vt_solver_sync(vt_solver* s);
+
+/* Number of particles registered so far. */
+vt_status vt_solver_num_particles(const vt_solver* s, uint32_t* out);
+
+/* State access: `count` particles from `first`, as (x, y, z) triples.  With
+ * *_on_device = 0 the buffer is ordinary host memory and the call returns after the
+ * copy; with 1 it is any memory the device can address (device memory, or pinned /
+ * registered host memory) and the copy is only enqueued on `stream`.  The public
+ * buffers positions / normals / velocities of VtClothSolverGPU (:209-217). */
+vt_status vt_positions_get(vt_solver* s, uint32_t first, uint32_t count, float* dst,
+                           int32_t dst_on_device, void* stream);
+vt_status vt_normals_get(vt_solver* s, uint32_t first, uint32_t count, float* dst,
+                         int32_t dst_on_device, void* stream);
+vt_status vt_velocities_get(vt_solver* s, uint32_t first, uint32_t count, float* dst,
+                            int32_t dst_on_device, void* stream);
+vt_status vt_positions_set(vt_solver* s, uint32_t first, uint32_t count, const float* src,
+                           int32_t src_on_device, void* stream);
+vt_status vt_velocities_set(vt_solver* s, uint32_t first, uint32_t count, const float* src,
+                            int32_t src_on_device, void* stream);
+
+/* invMasses (:217), mutated by MouseGrabber (Velvet/MouseGrabber.hpp:45-60). */
+vt_status vt_inv_mass_get(vt_solver* s, uint32_t first, uint32_t count, float* dst);
+vt_status vt_inv_mass_set(vt_solver* s, uint32_t first, uint32_t count, const float* src);
+
+/* attachSlotPositions (:229), moved by scenes (Velvet/main.cpp:326-331). */
+vt_status vt_attach_slot_set(vt_solver* s, int32_t slot, const float xyz[3]);
+
+/* Debug views of the solver's spatial hash after the last hash build, in the
+ * reference's layouts: VT_DEBUG_PARTICLE_HASH / _PARTICLE_INDEX (sorted keys and
+ * particle ids, num_particles uint32 each), _CELL_START (table_size + 1), _CELL_END
+ * (table_size), _NEIGHBORS (max_num_neighbors * num_particles, column-major
+ * neighbors[id + k * num_particles], terminated by 0xffffffff), _PREDICTED (float3
+ * per particle).  `bytes` is the size of dst; the call fails if it is too small. */
+#define VT_DEBUG_PARTICLE_HASH  0
+#define VT_DEBUG_PARTICLE_INDEX 1
+#define VT_DEBUG_CELL_START     2
+#define VT_DEBUG_CELL_END       3
+#define VT_DEBUG_NEIGHBORS      4
+#define VT_DEBUG_PREDICTED      5
+#define VT_DEBUG_TABLE_SIZE     6   /* one int32 */
+vt_status vt_solver_debug_get(vt_solver* s, int32_t what, void* dst, uint64_t bytes);
+
+/* Kernel launches this solver has enqueued since it was created (every CUDA kernel of
+ * this library counts; memsets and copies do not). */
+vt_status vt_solver_launch_count(const vt_solver* s, uint64_t* out);
+
+/* Replay each frame's launches as one CUDA graph (default 1); 0 launches every kernel
+ * directly, as the reference does. */
+vt_status vt_solver_use_graphs(vt_solver* s, int32_t on);
+
+/* ------------------------------------------------------------------ batched solver
+ * Many independent cloths advanced together.  Each cloth is registered on its own
+ * vt_solver (the plain API above), then copied into the batch, where it keeps its own
+ * parameter block, spatial hash, colliders and attach slots: a cloth's result in the
+ * batch is bit-identical to the same vt_solver simulated alone.  (The reference has no
+ * isolated batching: several cloths added to one VtClothSolverGPU share one hash and
+ * collide with each other, Velvet/main.cpp:243-279; that form is the plain solver.)
+ * One frame of the whole batch is one CUDA graph launch of multi-cloth kernels. */
+typedef struct vt_batch vt_batch;
+
+vt_status vt_batch_create(vt_batch** out);
+vt_status vt_batch_destroy(vt_batch* b);
+
+/* Copies everything `cloth` has registered (particles, constraints, colliders, slots,
+ * parameters, current state) into the batch; *out_index receives its index.  The
+ * source solver may be destroyed afterwards. */
+vt_status vt_batch_add(vt_batch* b, vt_solver* cloth, int32_t* out_index);
+
+vt_status vt_batch_size(const vt_batch* b, int32_t* num_cloths, uint64_t* num_particles);
+
+/* Replaces the colliders of cloth `index` (same count as when it was added). */
+vt_status vt_batch_colliders_set(vt_batch* b, int32_t index, const vt_sdf_collider* colliders,
+                                 uint32_t count);
+
+/* Moves attach slot `slot` (cloth-local index) of cloth `index`. */
+vt_status vt_batch_attach_slot_set(vt_batch* b, int32_t index, int32_t slot, const float xyz[3]);
+
+/* One frame of every cloth, with the same frame arguments as vt_simulate.
+ * particle_diameters: one per cloth, or NULL to use each cloth's registered diameter. */
+vt_status vt_batch_simulate(vt_batch* b, float frame_dt, int32_t substeps, int32_t iterations,
+                            float relaxation, float friction, float collision_margin,
+                            const float* particle_diameters, void* stream);
+
+vt_status vt_batch_sync(vt_batch* b);
+
+/* Positions / normals / velocities of cloth `index` (all its particles), with the
+ * dst_on_device convention of vt_positions_get. */
+vt_status vt_batch_positions_get(vt_batch* b, int32_t index, float* dst, int32_t dst_on_device,
+                                 void* stream);
+vt_status vt_batch_normals_get(vt_batch* b, int32_t index, float* dst, int32_t dst_on_device,
+                               void* stream);
+vt_status vt_batch_velocities_get(vt_batch* b, int32_t index, float* dst, int32_t dst_on_device,
+                                  void* stream);
+/* All cloths' positions at once, cloth after cloth in index order. */
+vt_status vt_batch_all_positions_get(vt_batch* b, float* dst, int32_t dst_on_device, void* stream);
+
+/* Kernels enqueued by this batch so far (graph replays count their kernel nodes). */
+vt_status vt_batch_launch_count(const vt_batch* b, uint64_t* out);
+
+/* Use CUDA graphs for frames (default 1); 0 launches every kernel directly. */
+vt_status vt_batch_use_graphs(vt_batch* b, int32_t on);
+
+/* ------------------------------------------------------------------ profiler
+ * Per-stage GPU timing, the counterpart of the reference's ScopedTimerGPU labels
+ * (Velvet/Timer.hpp:95-151, 242-260): while enabled, every stage launch of every
+ * handle is bracketed by a pair of CUDA events on its stream.  vt_profiler_read waits
+ * for the recorded events and reports, per stage, the launches and the summed event
+ * time.  Process-wide; off by default. */
+typedef struct vt_stage_time {
+    char     name[32];
+    uint64_t launches;
+    double   total_ms;
+} vt_stage_time;
+
+vt_status vt_profiler_enable(int32_t on);
+vt_status vt_profiler_reset(void);
+/* Writes up to `capacity` entries; *count receives the number of stages with data. */
+vt_status vt_profiler_read(vt_stage_time* out, uint32_t capacity, uint32_t* count);
+
+/* ------------------------------------------------------------------ spatial hash */
+
+/* HashObjects (Velvet/SpatialHashGPU.cu:159-196) on caller-owned device buffers:
+ * hashes positions[num_objects] (float3) into cells of cell_spacing, sorts
+ * (key, index) pairs stably by key, fills cell_start[table_size + 1] (0xffffffff for
+ * empty cells) and cell_end[table_size] for occupied cells, and writes the column-major
+ * neighbour lists with the initial-position filter.  Sort scratch space is allocated
+ * on first use per device and kept until the library is unloaded (the reference keeps
+ * a static cub buffer).  Enqueued on `stream`. */
+vt_status vt_hash_objects(uint32_t* particle_hash, uint32_t* particle_index,
+                          uint32_t* cell_start, uint32_t* cell_end, uint32_t* neighbors,
+                          const float* positions, const float* original_positions,
+                          const vt_hash_params* params, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VELVET_GB300_H */

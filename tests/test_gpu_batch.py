@@ -1,0 +1,87 @@
+"""GPU: the batched solver.  Each cloth in a batch must give exactly the bits it gives
+alone on the plain solver (and therefore exactly the oracle's bits): isolation of the
+per-cloth hash domains, parameters and colliders, with uneven cloth sizes."""
+import numpy as np
+import pytest
+
+import velvet_gb300 as vg
+from velvet_gb300 import workloads as W
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def mixed(count=7, seed=3):
+    return W.batched(count, frames=8, seed=seed, lo=8, hi=40)
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_batch_equals_each_cloth_alone(graphs):
+    wl = mixed()
+    batch = vg.BatchSolver()
+    batch.use_graphs(graphs)
+    alone = []
+    for spec in wl.cloths:
+        s = vg.ClothSolver()
+        W.build_plain(spec, s)
+        batch.add(s)
+        o = vg.ClothSolver()
+        W.build_plain(spec, o)
+        alone.append((o, spec))
+    for f in range(wl.frames):
+        batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin)
+        for o, spec in alone:
+            o.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin, spec.particle_diameter())
+    batch.sync()
+    for k, (o, spec) in enumerate(alone):
+        o.sync()
+        assert np.array_equal(bits(batch.positions(k)), bits(o.positions())), f"cloth {k} positions"
+        assert np.array_equal(bits(batch.velocities(k)), bits(o.velocities())), f"cloth {k} velocities"
+        assert np.array_equal(bits(batch.normals(k)), bits(o.normals())), f"cloth {k} normals"
+
+
+def test_batch_matches_oracle_with_moving_collider():
+    wl = mixed(3, seed=5)
+    batch = vg.BatchSolver()
+    ors = []
+    mover = W.moving_sphere(0.2, 0.3, 1.0)
+    for spec in wl.cloths:
+        spec.colliders = mover
+        s = vg.ClothSolver()
+        W.build_plain(spec, s)
+        batch.add(s)
+        o = Oracle()
+        W.build_plain(spec, o)
+        ors.append((o, spec))
+    for f in range(6):
+        for k, (o, spec) in enumerate(ors):
+            batch.update_colliders(k, spec.colliders(f))
+            o.update_colliders(spec.colliders(f))
+            o.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin, spec.particle_diameter())
+        batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin)
+    batch.sync()
+    for k, (o, _) in enumerate(ors):
+        assert np.array_equal(bits(batch.positions(k)), bits(o.positions())), f"cloth {k}"
+
+
+def test_batch_launch_count_is_per_frame_not_per_cloth():
+    wl = mixed(5)
+    batch = vg.BatchSolver()
+    for spec in wl.cloths:
+        s = vg.ClothSolver()
+        W.build_plain(spec, s)
+        batch.add(s)
+    batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin)
+    n1 = batch.launch_count()
+    batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin)
+    batch.sync()
+    per_frame = batch.launch_count() - n1
+    assert per_frame == n1 and per_frame < 40 + 3 * wl.substeps * wl.iterations

@@ -1,0 +1,381 @@
+// vt_hash.cu — spatial hash for self-collision: cell keys, a stable LSD radix sort of
+// (key, particle) pairs, cell start/end ranges and cached neighbour lists.
+//
+// Follows Velvet/SpatialHashGPU.cu:13-196:
+//   key   = abs(((ix*92837111) ^ (iy*689287499) ^ (iz*283923481)) % T),
+//           ix = (int)floor(x / cellSpacing) with IEEE division (no reciprocal),
+//           int32 products wrapping;
+//   sort  = stable by key (the reference uses cub::DeviceRadixSort::SortPairs; here a
+//           hand-written LSD radix sort: per-tile digit histograms, per-digit scan over
+//           tiles, then a scatter whose ranks come from warp match-any + per-warp
+//           counters, so equal digits keep index order);
+//   cells = cellStart[h] / cellEnd[h] of every occupied bucket, 0xffffffff elsewhere;
+//   lists = 27 buckets in x, y, z loop order, at most maxNumNeighbors entries read per
+//           bucket, pairs kept if |p_i - p_j|^2 < cellSpacing^2 and the initial
+//           positions are more than one diameter apart, column-major
+//           neighbors[id + k * N], 0xffffffff-terminated unless full.  Two of the 27
+//           cells that hash to the same bucket are visited twice, as in the reference.
+// In the multi-domain form each domain hashes into its own bucket range
+// [table_base, table_base + T) so one sort serves all domains and each domain's order
+// equals the order it would have alone.
+#include "vt_math.cuh"
+#include "vt_world.h"
+
+namespace vt {
+
+static constexpr int kBlock = 256;
+
+__device__ __forceinline__ int32_t int_coord(float v, float spacing)
+{
+    return (int32_t)floorf(v / spacing);
+}
+
+__device__ __forceinline__ uint32_t hash_coords(int32_t x, int32_t y, int32_t z, int32_t table)
+{
+    const uint32_t h = ((uint32_t)x * 92837111u) ^ ((uint32_t)y * 689287499u) ^
+                       ((uint32_t)z * 283923481u);
+    const int32_t r = ((int32_t)h) % table;
+    return (uint32_t)(r < 0 ? -r : r);
+}
+
+// ------------------------------------------------------------------ keys
+__global__ void __launch_bounds__(kBlock)
+k_hash_keys(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+            const float4* __restrict__ p, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int i = tl.begin + (int)threadIdx.x;
+    if (i >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    const float4 q = p[i];
+    const float sp = D.cell_spacing;
+    keys[i] = (uint32_t)D.table_base +
+              hash_coords(int_coord(q.x, sp), int_coord(q.y, sp), int_coord(q.z, sp), D.table_size);
+    vals[i] = (uint32_t)i;
+}
+
+// float3 input, one domain (the HashObjects entry point)
+__global__ void __launch_bounds__(kBlock)
+k_hash_keys_f3(const float* __restrict__ pos, int32_t n, float sp, int32_t table,
+               uint32_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+    const int i = blockIdx.x * kBlock + (int)threadIdx.x;
+    if (i >= n) return;
+    keys[i] = hash_coords(int_coord(pos[3 * i], sp), int_coord(pos[3 * i + 1], sp),
+                          int_coord(pos[3 * i + 2], sp), table);
+    vals[i] = (uint32_t)i;
+}
+
+// ------------------------------------------------------------------ radix sort
+static constexpr int kRsItems = 16;
+static constexpr int kRsWarps = kBlock / 32;
+static constexpr int kRsTile = kBlock * kRsItems;  // 4096 pairs per tile
+
+size_t radix_hist_words(int32_t n)
+{
+    const int64_t tiles = (n + kRsTile - 1) / kRsTile;
+    return (size_t)(tiles > 0 ? tiles : 1) * 256 + 256;
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_rs_upsweep(const uint32_t* __restrict__ keys, int32_t n, int shift, int nbits,
+             uint32_t* __restrict__ hist, int32_t ntiles)
+{
+    __shared__ uint32_t h[256];
+    const int ndig = 1 << nbits;
+    for (int k = threadIdx.x; k < ndig; k += kBlock) h[k] = 0;
+    __syncthreads();
+    const uint32_t mask = (uint32_t)ndig - 1;
+    const int base = blockIdx.x * kRsTile;
+#pragma unroll 4
+    for (int j = 0; j < kRsItems; ++j) {
+        const int idx = base + j * kBlock + (int)threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & mask], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < ndig; k += kBlock) hist[(size_t)k * ntiles + blockIdx.x] = h[k];
+}
+
+// Block-wide exclusive scan of one value per thread (kBlock threads); returns the
+// exclusive prefix, *total gets the block sum.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total)
+{
+    __shared__ uint32_t warp_sums[kRsWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t wpre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < kRsWarps; ++w) {
+        const uint32_t s = warp_sums[w];
+        if (w < warp) wpre += s;
+        tot += s;
+    }
+    __syncthreads();
+    *total = tot;
+    return wpre + incl - v;
+}
+
+// One block per digit: exclusive scan of that digit's counts over the tiles.
+__global__ void __launch_bounds__(kBlock)
+k_rs_scan(uint32_t* __restrict__ hist, int32_t ntiles, uint32_t* __restrict__ digit_tot)
+{
+    uint32_t* row = hist + (size_t)blockIdx.x * ntiles;
+    uint32_t carry = 0;
+    for (int base = 0; base < ntiles; base += kBlock) {
+        const int idx = base + (int)threadIdx.x;
+        const uint32_t v = idx < ntiles ? row[idx] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, &tot);
+        if (idx < ntiles) row[idx] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) digit_tot[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int32_t n, int shift,
+               int nbits, const uint32_t* __restrict__ hist, const uint32_t* __restrict__ digit_tot,
+               int32_t ntiles)
+{
+    __shared__ uint32_t off[256];
+    __shared__ uint32_t wcnt[kRsWarps][256];
+    const int ndig = 1 << nbits;
+    const uint32_t mask = (uint32_t)ndig - 1;
+    {
+        const uint32_t t = (int)threadIdx.x < ndig ? digit_tot[threadIdx.x] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(t, &tot);
+        if ((int)threadIdx.x < ndig)
+            off[threadIdx.x] = ex + hist[(size_t)threadIdx.x * ntiles + blockIdx.x];
+    }
+    for (int k = threadIdx.x; k < kRsWarps * 256; k += kBlock) (&wcnt[0][0])[k] = 0;
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    const int wbase = blockIdx.x * kRsTile + warp * (32 * kRsItems);
+    uint32_t mk[kRsItems], mv[kRsItems], mr[kRsItems];
+#pragma unroll
+    for (int j = 0; j < kRsItems; ++j) {
+        const int idx = wbase + j * 32 + lane;
+        const bool valid = idx < n;
+        const uint32_t key = valid ? kin[idx] : 0u;
+        const uint32_t val = valid ? vin[idx] : 0u;
+        const uint32_t d = valid ? ((key >> shift) & mask) : 0x100u;  // 0x100: not a digit
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t rank = 0;
+        if (valid) rank = wcnt[warp][d] + __popc(peers & lt);
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] += __popc(peers);
+        __syncwarp();
+        mk[j] = key;
+        mv[j] = val;
+        mr[j] = rank;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < ndig) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kRsWarps; ++w) {
+            const uint32_t c = wcnt[w][threadIdx.x];
+            wcnt[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRsItems; ++j) {
+        const int idx = wbase + j * 32 + lane;
+        if (idx < n) {
+            const uint32_t d = (mk[j] >> shift) & mask;
+            const uint32_t pos = off[d] + wcnt[warp][d] + mr[j];
+            kout[pos] = mk[j];
+            vout[pos] = mv[j];
+        }
+    }
+}
+
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
+                             uint32_t* hist, uint32_t* digit_tot, int32_t n, int32_t bits,
+                             cudaStream_t st)
+{
+    if (n <= 1 || bits <= 0) return cudaSuccess;
+    const int passes = (bits + 7) / 8;
+    const int per = (bits + passes - 1) / passes;
+    const int32_t ntiles = (n + kRsTile - 1) / kRsTile;
+    uint32_t *ki = keys, *vi = vals, *ko = keys_tmp, *vo = vals_tmp;
+    int shift = 0;
+    for (int ps = 0; ps < passes; ++ps) {
+        const int nb = (bits - shift) < per ? (bits - shift) : per;
+        k_rs_upsweep<<<ntiles, kBlock, 0, st>>>(ki, n, shift, nb, hist, ntiles);
+        k_rs_scan<<<1 << nb, kBlock, 0, st>>>(hist, ntiles, digit_tot);
+        k_rs_downsweep<<<ntiles, kBlock, 0, st>>>(ki, vi, ko, vo, n, shift, nb, hist, digit_tot, ntiles);
+        uint32_t* t;
+        t = ki; ki = ko; ko = t;
+        t = vi; vi = vo; vo = t;
+        shift += nb;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (ki != keys) {
+        e = cudaMemcpyAsync(keys, ki, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+        e = cudaMemcpyAsync(vals, vi, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+    }
+    return e;
+}
+
+// ------------------------------------------------------------------ cell ranges
+// FindCellStart_Kernel, SpatialHashGPU.cu:44-77 (cell_start pre-filled with 0xff bytes)
+__global__ void __launch_bounds__(kBlock)
+k_cell_ranges(const uint32_t* __restrict__ keys, int32_t n, uint32_t* __restrict__ cs,
+              uint32_t* __restrict__ ce)
+{
+    const int t = blockIdx.x * kBlock + (int)threadIdx.x;
+    if (t >= n) return;
+    const uint32_t h = keys[t];
+    if (t == 0 || keys[t - 1] != h) {
+        cs[h] = (uint32_t)t;
+        if (t > 0) ce[keys[t - 1]] = (uint32_t)t;
+    }
+    if (t == n - 1) ce[h] = (uint32_t)n;
+}
+
+cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_start,
+                               uint32_t* cell_end, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_cell_ranges<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(keys, n, cell_start, cell_end);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ neighbour cache
+// CacheNeighbors_Kernel, SpatialHashGPU.cu:79-130, for sorted slot t.
+template <typename Pos>
+__device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* __restrict__ vals,
+                                                    const uint32_t* __restrict__ cs,
+                                                    const uint32_t* __restrict__ ce, Pos pos, Pos orig,
+                                                    uint32_t* __restrict__ out_base, uint32_t id_base,
+                                                    int32_t n, int32_t table_base, int32_t table,
+                                                    float sp, float sp2, float diam2, int32_t max_nbr)
+{
+    const uint32_t id = vals[t];
+    const vec3 position = pos(id);
+    const vec3 originalp = orig(id);
+    const int32_t ix = int_coord(position.x, sp), iy = int_coord(position.y, sp),
+                  iz = int_coord(position.z, sp);
+    uint32_t* out = out_base + (id - id_base);
+    int cnt = 0;
+    for (int32_t x = ix - 1; x <= ix + 1; ++x)
+        for (int32_t y = iy - 1; y <= iy + 1; ++y)
+            for (int32_t z = iz - 1; z <= iz + 1; ++z) {
+                const uint32_t h = (uint32_t)table_base + hash_coords(x, y, z, table);
+                const uint32_t start = cs[h];
+                if (start == 0xffffffffu) continue;
+                uint32_t end = ce[h];
+                const uint32_t lim = start + (uint32_t)max_nbr;
+                if (lim < end) end = lim;
+                for (uint32_t k = start; k < end; ++k) {
+                    const uint32_t nb = vals[k];
+                    const vec3 d1 = position - pos(nb);
+                    const vec3 d2 = originalp - orig(nb);
+                    if (nb != id && dot(d1, d1) < sp2 && dot(d2, d2) > diam2) {
+                        out[(size_t)cnt * n] = nb;
+                        ++cnt;
+                        if (cnt >= max_nbr) return;
+                    }
+                }
+            }
+    out[(size_t)cnt * n] = 0xffffffffu;
+}
+
+struct PosF4 {
+    const float4* __restrict__ a;
+    __device__ __forceinline__ vec3 operator()(uint32_t i) const { return xyz(a[i]); }
+};
+struct PosF3 {
+    const float* __restrict__ a;
+    __device__ __forceinline__ vec3 operator()(uint32_t i) const
+    {
+        return mk3(a[3 * (size_t)i], a[3 * (size_t)i + 1], a[3 * (size_t)i + 2]);
+    }
+};
+
+__global__ void __launch_bounds__(kBlock)
+k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+                  const uint32_t* __restrict__ vals, const uint32_t* __restrict__ cs,
+                  const uint32_t* __restrict__ ce, const float4* __restrict__ p,
+                  const float4* __restrict__ x0, uint32_t* __restrict__ nbr)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int t = tl.begin + (int)threadIdx.x;
+    if (t >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF4{p}, PosF4{x0}, nbr + D.nbr_base,
+                        (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
+                        D.cell_spacing, D.cell_spacing2, D.diameter2, D.max_nbr);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_cache_neighbors_f3(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ cs,
+                     const uint32_t* __restrict__ ce, const float* __restrict__ pos,
+                     const float* __restrict__ orig, uint32_t* __restrict__ nbr, int32_t n,
+                     int32_t table, float sp, float sp2, float diam2, int32_t max_nbr)
+{
+    const int t = blockIdx.x * kBlock + (int)threadIdx.x;
+    if (t >= n) return;
+    cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF3{pos}, PosF3{orig}, nbr, 0u, n, 0, table,
+                        sp, sp2, diam2, max_nbr);
+}
+
+cudaError_t launch_hash_keys(const Launch& L, int pin)
+{
+    if (!L.n_ptiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+    k_hash_keys<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.p[pin], d.keys, d.vals);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cache_neighbors(const Launch& L, int pin)
+{
+    if (!L.n_ptiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+    k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.vals, d.cell_start,
+                                                       d.cell_end, d.p[pin], d.x0, d.nbr);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ HashObjects (float3)
+// The whole HashObjects pipeline on caller buffers; scratch passed in.
+cudaError_t hash_objects_f3(uint32_t* phash, uint32_t* pindex, uint32_t* cell_start,
+                            uint32_t* cell_end, uint32_t* neighbors, const float* positions,
+                            const float* original, const vt_hash_params& hp,
+                            uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* hist,
+                            uint32_t* digit_tot, cudaStream_t st)
+{
+    const int32_t n = (int32_t)hp.num_objects;
+    cudaError_t e = cudaMemsetAsync(cell_start, 0xff, sizeof(uint32_t) * ((size_t)hp.table_size + 1), st);
+    if (e != cudaSuccess || n == 0) return e;
+    const int blocks = (n + kBlock - 1) / kBlock;
+    k_hash_keys_f3<<<blocks, kBlock, 0, st>>>(positions, n, hp.cell_spacing, hp.table_size, phash, pindex);
+    int bits = 0;
+    while ((1ll << bits) < (long long)hp.table_size) ++bits;  // ceil(log2(tableSize))
+    e = radix_sort_pairs(phash, pindex, keys_tmp, vals_tmp, hist, digit_tot, n, bits, st);
+    if (e != cudaSuccess) return e;
+    k_cell_ranges<<<blocks, kBlock, 0, st>>>(phash, n, cell_start, cell_end);
+    k_cache_neighbors_f3<<<blocks, kBlock, 0, st>>>(pindex, cell_start, cell_end, positions, original,
+                                                    neighbors, n, hp.table_size, hp.cell_spacing,
+                                                    hp.cell_spacing2, hp.particle_diameter2,
+                                                    (int32_t)hp.max_num_neighbors);
+    return cudaGetLastError();
+}
+
+}  // namespace vt

@@ -1,0 +1,490 @@
+// vt_kernels.cu — XPBD substep kernels for sm_103a.
+//
+// Same arithmetic as the reference kernels (Velvet/VtClothSolverGPU.cu), different
+// packaging:
+//   * Jacobi sums are gathers, not atomics.  Each particle walks its constraints in
+//     constraint order (CSR built at registration) and adds their corrections in that
+//     order, so the sum is the one a sequential run of the reference kernels produces
+//     and is identical from run to run.  Stretch and attachment corrections are
+//     recomputed by each endpoint (the two endpoints of a stretch constraint get exact
+//     negatives of each other's intermediate values, so the recomputation is exact);
+//     bending is evaluated once per constraint into per-corner slots that the particle
+//     gather reads.
+//   * ApplyDeltas is fused into the gather that produces the deltas; predicted
+//     positions ping-pong between two buffers so every constraint of an iteration sees
+//     the positions of the previous iteration, as the reference's launch order implies.
+//   * CollideParticles + ApplyDeltas + CollideSDF are one kernel; Finalize and the next
+//     substep's PredictPositions are fused into the last iteration's gather; the
+//     pre-stabilisation CollideSDF is fused with the first PredictPositions.
+//   * float4 particles (w = inverse mass) so each particle is one 16-byte load.
+#include "vt_math.cuh"
+#include "vt_world.h"
+
+namespace vt {
+
+static constexpr int kBlock = 256;
+
+// ------------------------------------------------------------------ colliders
+__device__ __forceinline__ float sgnf(float v) { return (v > 0) ? 1.0f : (v < 0 ? -1.0f : 0.0f); }
+
+// SDFCollider::ComputeSDF, Velvet/VtClothSolverGPU.cuh:22-89
+__device__ vec3 collider_sdf(const ColliderDev& c, vec3 t, float margin)
+{
+    if (c.type == 1) {  // plane
+        float offset = t.y - (c.py + margin);
+        if (offset < 0) return mk3(0, -offset, 0);
+    } else if (c.type == 0) {  // sphere
+        float radius = c.sx + margin;
+        vec3 diff = t - mk3(c.px, c.py, c.pz);
+        float distance = length(diff);
+        float offset = distance - radius;
+        if (offset < 0) {
+            vec3 direction = diff / distance;
+            return direction * (-offset);
+        }
+    } else if (c.type == 2) {  // cube
+        vec3 correction = mk3(0, 0, 0);
+        vec3 local = m4v3(c.inv, t, 1.0f);
+        vec3 cube = mk3(0.5f + margin / c.sx, 0.5f + margin / c.sy, 0.5f + margin / c.sz);
+        vec3 offset = mk3(fabsf(local.x), fabsf(local.y), fabsf(local.z)) - cube;
+        float maxv = fmaxf(offset.x, fmaxf(offset.y, offset.z));
+        float minv = fminf(offset.x, fminf(offset.y, offset.z));
+        float midv = ((offset.x + offset.y) + offset.z - maxv) - minv;
+        float scalar = 1.0f;
+        if (maxv < 0) {
+            const float m = 0.03f;
+            if (midv > -m) scalar = 0.2f;
+            if (minv > -m) {
+                vec3 mask = mk3(offset.x < 0 ? sgnf(local.x) : 0, offset.y < 0 ? sgnf(local.y) : 0,
+                                offset.z < 0 ? sgnf(local.z) : 0);
+                vec3 vec = offset + mk3(m, m, m);
+                float len = length(vec);
+                if (len < m) correction = cmul(mask, normalize(vec)) * (m - len);
+            } else if (offset.x == maxv) {
+                correction = mk3(copysignf(-offset.x, local.x), 0, 0);
+            } else if (offset.y == maxv) {
+                correction = mk3(0, copysignf(-offset.y, local.y), 0);
+            } else if (offset.z == maxv) {
+                correction = mk3(0, 0, copysignf(-offset.z, local.z));
+            }
+        }
+        float ms[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) ms[k] = c.cur3[k] * scalar;
+        return m3v3(ms, correction);
+    }
+    return mk3(0, 0, 0);
+}
+
+// ComputeFriction, Velvet/VtClothSolverGPU.cu:272-287
+__device__ __forceinline__ vec3 friction_of(vec3 corr, vec3 relvel, float friction)
+{
+    vec3 fr = mk3(0, 0, 0);
+    float cl = length(corr);
+    if (friction > 0 && cl > 0) {
+        vec3 nrm = corr / cl;
+        vec3 tan = relvel - nrm * dot(relvel, nrm);
+        float tl = length(tan);
+        float mt = cl * friction;
+        fr = (-tan) * fminf(mt / tl, 1.0f);
+    }
+    return fr;
+}
+
+// CollideSDF_Kernel body, Velvet/VtClothSolverGPU.cu:289-314
+__device__ __forceinline__ vec3 collide_sdf(const DomainParams& D, const ColliderDev* __restrict__ cols,
+                                            vec3 pred, vec3 pos, float dt)
+{
+    for (int k = 0; k < D.col_count; ++k) {
+        const ColliderDev& c = cols[D.col_begin + k];
+        vec3 corr = collider_sdf(c, pred, D.margin);
+        pred = pred + corr;
+        if (dot(corr, corr) > 0) {
+            // VelocityAt, VtClothSolverGPU.cuh:91-96 (last * invCur precomputed)
+            vec3 lp = m4v3(c.last_inv, pred, 1.0f);
+            vec3 vel = (pred - lp) / c.delta_time;
+            vec3 relvel = (pred - pos) - vel * dt;
+            pred = pred + friction_of(corr, relvel, D.friction);
+        }
+    }
+    return pred;
+}
+
+__device__ __forceinline__ void flag_nonfinite(int32_t* status, const DomainParams& D, int dom, vec3 a)
+{
+    if (!(isfinite(a.x) && isfinite(a.y) && isfinite(a.z))) {
+        atomicOr(&status[0], 1);
+        atomicOr(&status[1 + dom], 1);
+    }
+}
+
+// ------------------------------------------------------------------ pre-stabilisation + predict
+// CollideSDF(positions, ..., frameDt) (VtClothSolverGPU.hpp:73) then PredictPositions
+// (VtClothSolverGPU.cu:42-53) of substep 0.
+__global__ void __launch_bounds__(kBlock)
+k_presdf_predict(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+                 const ColliderDev* __restrict__ cols, float4* __restrict__ x, float4* __restrict__ v,
+                 float4* __restrict__ pout)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int i = tl.begin + (int)threadIdx.x;
+    if (i >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    float4 x4 = x[i];
+    vec3 pos = xyz(x4);
+    if (D.col_count > 0) {
+        pos = collide_sdf(D, cols, pos, pos, D.dt_frame);
+        x[i] = make_float4(pos.x, pos.y, pos.z, x4.w);
+    }
+    const float dt = D.dt_sub;
+    vec3 vel = xyz(v[i]);
+    vel = vel + mk3(D.gx, D.gy, D.gz) * dt;
+    vec3 pred = pos + vel * dt;
+    v[i] = make_float4(vel.x, vel.y, vel.z, 0.0f);
+    pout[i] = make_float4(pred.x, pred.y, pred.z, x4.w);
+}
+
+// ------------------------------------------------------------------ collide particles + SDF
+// CollideParticles_Kernel (VtClothSolverGPU.cu:329-373) + ApplyDeltas (:253-264) +
+// CollideSDF (:289-314) for one substep.
+__global__ void __launch_bounds__(kBlock)
+k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+          const ColliderDev* __restrict__ cols, const float4* __restrict__ x,
+          const float4* __restrict__ pin, float4* __restrict__ pout,
+          const uint32_t* __restrict__ nbr)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int i = tl.begin + (int)threadIdx.x;
+    if (i >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    const float4 pi4 = pin[i];
+    vec3 pi = xyz(pi4);
+    const float wi = pi4.w;
+    const vec3 xi = xyz(x[i]);
+    if (D.self_collision) {
+        vec3 delta = mk3(0, 0, 0);
+        int count = 0;
+        const vec3 veli = pi - xi;
+        const uint32_t* nb = nbr + D.nbr_base + (i - D.p_begin);
+        const int stride = D.p_count;
+        const float diam = D.diameter;
+        for (int k = 0; k < D.max_nbr; ++k) {
+            const uint32_t j = __ldg(nb + (size_t)k * stride);
+            if (j == 0xffffffffu) break;
+            const float4 pj4 = pin[j];
+            const float denom = wi + pj4.w;
+            if (denom <= 0) continue;
+            const vec3 pj = xyz(pj4);
+            const vec3 diff = pi - pj;
+            const float d = length(diff);
+            if (d >= diam) continue;
+            const vec3 grad = diff / (d + VT_EPSILON);
+            const float lambda = (d - diam) / denom;
+            const vec3 common = grad * lambda;
+            count++;
+            delta = delta - common * wi;
+            const vec3 relvel = veli - (pj - xyz(x[j]));
+            const vec3 fr = friction_of(common, relvel, D.friction);
+            delta = delta + fr * wi;
+        }
+        if (count > 0) {
+            const float c = (float)count;
+            pi = pi + (delta / c) * D.relax;
+        }
+    }
+    pi = collide_sdf(D, cols, pi, xi, D.dt_sub);
+    pout[i] = make_float4(pi.x, pi.y, pi.z, wi);
+}
+
+// ------------------------------------------------------------------ bending
+// SolveBending_Kernel (VtClothSolverGPU.cu:117-189), once per constraint; the four
+// corrections go to per-corner slots (w = 1 when the constraint fired).
+__global__ void __launch_bounds__(kBlock)
+k_bend(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+       const float4* __restrict__ pin, const uint4* __restrict__ bidx,
+       const float* __restrict__ brest, float4* __restrict__ bcorr)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int b = tl.begin + (int)threadIdx.x;
+    if (b >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    const uint4 q = bidx[b];
+    const float rest = brest[b];
+    const float4 a0 = pin[q.x], a1 = pin[q.y], a2 = pin[q.z], a3 = pin[q.w];
+    const vec3 p0 = xyz(a0), p1 = xyz(a1), p2 = xyz(a2), p3 = xyz(a3);
+    const float w0 = a0.w, w1 = a1.w, w2 = a2.w, w3 = a3.w;
+    float4 c0 = make_float4(0, 0, 0, 0), c1 = c0, c2 = c0, c3 = c0;
+    const vec3 e = p3 - p2;
+    const float elen = length(e);
+    if (!(elen < VT_EPSILON)) {
+        const float inv = 1.0f / elen;
+        vec3 n1 = cross(p2 - p0, p3 - p0);
+        n1 = n1 / dot(n1, n1);
+        vec3 n2 = cross(p3 - p1, p2 - p1);
+        n2 = n2 / dot(n2, n2);
+        const vec3 d0 = n1 * elen;
+        const vec3 d1 = n2 * elen;
+        const vec3 d2 = n1 * (dot(p0 - p3, e) * inv) + n2 * (dot(p1 - p3, e) * inv);
+        const vec3 d3 = n1 * (dot(p2 - p0, e) * inv) + n2 * (dot(p2 - p1, e) * inv);
+        n1 = normalize(n1);
+        n2 = normalize(n2);
+        const float phi = vt_acosf(gclamp(dot(n1, n2), -1.0f, 1.0f));
+        float lambda = w0 * dot(d0, d0) + w1 * dot(d1, d1);
+        lambda = lambda + w2 * dot(d2, d2);
+        lambda = lambda + w3 * dot(d3, d3);
+        if (!(lambda < VT_EPSILON)) {
+            const float dt = D.dt_sub;
+            const float xpbd = D.bend_compliance / dt / dt;
+            lambda = (phi - rest) / (lambda + xpbd);
+            if (dot(cross(n1, n2), e) > 0.0f) lambda = -lambda;
+            vec3 k0 = d0 * (-w0 * lambda), k1 = d1 * (-w1 * lambda);
+            vec3 k2 = d2 * (-w2 * lambda), k3 = d3 * (-w3 * lambda);
+            c0 = make_float4(k0.x, k0.y, k0.z, 1.0f);
+            c1 = make_float4(k1.x, k1.y, k1.z, 1.0f);
+            c2 = make_float4(k2.x, k2.y, k2.z, 1.0f);
+            c3 = make_float4(k3.x, k3.y, k3.z, 1.0f);
+        }
+    }
+    float4* out = bcorr + 4 * (size_t)b;
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+// ------------------------------------------------------------------ constraint gather
+// SolveStretch (:65-102) + SolveAttachment (:205-235) + the bending corners written by
+// k_bend, summed per particle in constraint order, then ApplyDeltas (:253-264).  With
+// `fin` set, Finalize (:388-407) follows, and with SOLVE_FINALIZE_PREDICT the next
+// substep's PredictPositions (:42-53).
+template <int kMode>
+__global__ void __launch_bounds__(kBlock)
+k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+        const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ x,
+        float4* __restrict__ v, const float4* __restrict__ x0,
+        const int32_t* __restrict__ st_off, const int2* __restrict__ st_ent,
+        const int32_t* __restrict__ at_off, const int2* __restrict__ at_ent,
+        const LraGroup* __restrict__ lra, const float4* __restrict__ slots,
+        const float4* __restrict__ slots0, const int32_t* __restrict__ bd_off,
+        const int32_t* __restrict__ bd_ent, const float4* __restrict__ bcorr,
+        int32_t* __restrict__ status)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int i = tl.begin + (int)threadIdx.x;
+    if (i >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    const float4 pi4 = pin[i];
+    vec3 pi = xyz(pi4);
+    const float wi = pi4.w;
+    vec3 acc = mk3(0, 0, 0);
+    int cnt = 0;
+
+    // stretch: each entry is (other particle, rest length)
+    {
+        const int e0 = st_off[i], e1 = st_off[i + 1];
+        for (int e = e0; e < e1; ++e) {
+            const int2 en = st_ent[e];
+            const float4 pj4 = pin[en.x];
+            const float rest = __int_as_float(en.y);
+            const vec3 diff = pi - xyz(pj4);
+            const float d = length(diff);
+            const float denom = wi + pj4.w;
+            if (d != rest && denom > 0) {
+                const vec3 grad = diff / (d + VT_EPSILON);
+                const float lambda = (d - rest) / denom;
+                const vec3 common = grad * lambda;
+                acc3(acc, common * (-wi));
+                cnt++;
+            }
+        }
+    }
+    // attachments: (slot, distance) or an LRA group (distances recomputed from x0)
+    {
+        const int e0 = at_off[i], e1 = at_off[i + 1];
+        const float lrs = D.lrs;
+        for (int e = e0; e < e1; ++e) {
+            const int2 en = at_ent[e];
+            if (en.x >= 0) {
+                const float target = __int_as_float(en.y) * lrs;
+                if (wi == 0 && target > 0) continue;
+                const vec3 diff = pi - xyz(slots[en.x]);
+                const float d = length(diff);
+                if (d > target) {
+                    acc3(acc, (-diff) + (diff / d) * target);
+                    cnt++;
+                }
+            } else {
+                const LraGroup g = lra[-en.x - 1];
+                const vec3 x0i = xyz(x0[i]);
+                for (int s = g.slot_begin; s < g.slot_begin + g.slot_count; ++s) {
+                    const float rest = length(xyz(slots0[s]) - x0i);
+                    const float target = rest * lrs;
+                    if (wi == 0 && target > 0) continue;
+                    const vec3 diff = pi - xyz(slots[s]);
+                    const float d = length(diff);
+                    if (d > target) {
+                        acc3(acc, (-diff) + (diff / d) * target);
+                        cnt++;
+                    }
+                }
+            }
+        }
+    }
+    // bending corners
+    {
+        const int e0 = bd_off[i], e1 = bd_off[i + 1];
+        for (int e = e0; e < e1; ++e) {
+            const float4 c = bcorr[bd_ent[e]];
+            if (c.w != 0.0f) {
+                acc3(acc, xyz(c));
+                cnt++;
+            }
+        }
+    }
+    if (cnt > 0) {
+        const float count = (float)cnt;
+        pi = pi + (acc / count) * D.relax;
+    }
+    if (kMode == SOLVE_PLAIN) {
+        pout[i] = make_float4(pi.x, pi.y, pi.z, wi);
+        return;
+    }
+    // Finalize
+    const float dt = D.dt_sub;
+    const float4 x4 = x[i];
+    const vec3 xi = xyz(x4);
+    vec3 np = pi;
+    vec3 rv = (np - xi) / dt;
+    const float rl = length(rv);
+    if (rl > D.max_speed) {
+        rv = (rv / rl) * D.max_speed;
+        np = xi + rv * dt;
+    }
+    vec3 vn = rv * (1.0f - D.damping * dt);
+    flag_nonfinite(status, D, tl.dom, np);
+    x[i] = make_float4(np.x, np.y, np.z, x4.w);
+    if (kMode == SOLVE_FINALIZE_PREDICT) {
+        vn = vn + mk3(D.gx, D.gy, D.gz) * dt;
+        pi = np + vn * dt;
+    }
+    v[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
+    pout[i] = make_float4(pi.x, pi.y, pi.z, x4.w);
+}
+
+// Finalize without a preceding constraint gather (zero iterations).
+template <int kPredict>
+__global__ void __launch_bounds__(kBlock)
+k_finalize(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+           float4* __restrict__ p, float4* __restrict__ x, float4* __restrict__ v,
+           int32_t* __restrict__ status)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int i = tl.begin + (int)threadIdx.x;
+    if (i >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    const float dt = D.dt_sub;
+    const float4 x4 = x[i];
+    const vec3 xi = xyz(x4);
+    vec3 pi = xyz(p[i]);
+    vec3 np = pi;
+    vec3 rv = (np - xi) / dt;
+    const float rl = length(rv);
+    if (rl > D.max_speed) {
+        rv = (rv / rl) * D.max_speed;
+        np = xi + rv * dt;
+    }
+    vec3 vn = rv * (1.0f - D.damping * dt);
+    flag_nonfinite(status, D, tl.dom, np);
+    x[i] = make_float4(np.x, np.y, np.z, x4.w);
+    if (kPredict) {
+        vn = vn + mk3(D.gx, D.gy, D.gz) * dt;
+        pi = np + vn * dt;
+    }
+    v[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
+    p[i] = make_float4(pi.x, pi.y, pi.z, x4.w);
+}
+
+// ------------------------------------------------------------------ normals
+// ComputeTriangleNormals + ComputeVertexNormals (:419-465) as a per-vertex gather over
+// incident triangles in triangle order.
+__global__ void __launch_bounds__(kBlock)
+k_normals(const Tile* __restrict__ tiles, const float4* __restrict__ x,
+          const uint4* __restrict__ tri, const int32_t* __restrict__ tn_off,
+          const int32_t* __restrict__ tn_ent, float4* __restrict__ nrm)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int i = tl.begin + (int)threadIdx.x;
+    if (i >= tl.end) return;
+    vec3 acc = mk3(0, 0, 0);
+    const int e0 = tn_off[i], e1 = tn_off[i + 1];
+    for (int e = e0; e < e1; ++e) {
+        const uint4 t = tri[tn_ent[e]];
+        const vec3 p1 = xyz(x[t.x]), p2 = xyz(x[t.y]), p3 = xyz(x[t.z]);
+        acc3(acc, cross(p2 - p1, p3 - p1));
+    }
+    const vec3 n = normalize(acc);
+    nrm[i] = make_float4(n.x, n.y, n.z, 0.0f);
+}
+
+// ------------------------------------------------------------------ launchers
+cudaError_t launch_presdf_predict(const Launch& L, int pcur)
+{
+    if (!L.n_ptiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+    k_presdf_predict<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.col, d.x, d.v, d.p[pcur]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_collide(const Launch& L, int pin, int pout)
+{
+    if (!L.n_ptiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+    k_collide<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.col, d.x, d.p[pin], d.p[pout], d.nbr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bend(const Launch& L, int pin)
+{
+    if (!L.n_btiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+    k_bend<<<L.n_btiles, kBlock, 0, L.st>>>(d.btiles, d.dom, d.p[pin], d.bd_idx, d.bd_rest, d.bd_corr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve(const Launch& L, int pin, int pout, int mode)
+{
+    if (!L.n_ptiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+#define VT_SOLVE_ARGS                                                                      \
+    d.ptiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.st_off, d.st_ent, d.at_off,    \
+        d.at_ent, d.lra, d.slots, d.slots0, d.bd_off, d.bd_ent, d.bd_corr, d.status
+    if (mode == SOLVE_PLAIN)
+        k_solve<SOLVE_PLAIN><<<L.n_ptiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
+    else if (mode == SOLVE_FINALIZE)
+        k_solve<SOLVE_FINALIZE><<<L.n_ptiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
+    else
+        k_solve<SOLVE_FINALIZE_PREDICT><<<L.n_ptiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
+#undef VT_SOLVE_ARGS
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const Launch& L, int pcur, int predict_next)
+{
+    if (!L.n_ptiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+    if (predict_next)
+        k_finalize<1><<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.p[pcur], d.x, d.v, d.status);
+    else
+        k_finalize<0><<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.p[pcur], d.x, d.v, d.status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_normals(const Launch& L)
+{
+    if (!L.n_ptiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+    k_normals<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.x, d.tri, d.tn_off, d.tn_ent, d.nrm);
+    return cudaGetLastError();
+}
+
+}  // namespace vt

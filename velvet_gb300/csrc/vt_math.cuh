@@ -1,0 +1,120 @@
+// vt_math.cuh — FP32 vector arithmetic of the cloth solver, in the association order of
+// glm (the vector library of the reference solver, Velvet/VtClothSolverGPU.cu):
+//   dot(a, b)      = (a.x*b.x + a.y*b.y) + a.z*b.z
+//   length(v)      = sqrt(dot(v, v))
+//   normalize(v)   = v * (1 / sqrt(dot(v, v)))
+//   mat4 * vec4    = (c0*x + c1*y) + (c2*z + c3*w)
+//   mat3 * vec3    = (c0*x + c1*y) + c2*z
+// The translation units that include this file are compiled with -fmad=false, so no
+// multiply-add pair is contracted into an FMA: every result is the IEEE-rounded value
+// of the operations as written, on the device and in host code alike.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#define VT_HD __host__ __device__ __forceinline__
+#define VT_EPSILON 1e-6f  // EPSILON, Velvet/Common.cuh:12
+
+struct vec3 {
+    float x, y, z;
+};
+
+VT_HD vec3 mk3(float x, float y, float z) { vec3 r; r.x = x; r.y = y; r.z = z; return r; }
+VT_HD vec3 xyz(float4 a) { return mk3(a.x, a.y, a.z); }
+VT_HD vec3 operator+(vec3 a, vec3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+VT_HD vec3 operator-(vec3 a, vec3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+VT_HD vec3 operator-(vec3 a) { return mk3(-a.x, -a.y, -a.z); }
+VT_HD vec3 operator*(vec3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+VT_HD vec3 operator/(vec3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+VT_HD vec3 cmul(vec3 a, vec3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
+VT_HD float dot(vec3 a, vec3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+VT_HD float length(vec3 a) { return sqrtf(dot(a, a)); }
+VT_HD vec3 normalize(vec3 a) { return a * (1.0f / sqrtf(dot(a, a))); }
+VT_HD vec3 cross(vec3 a, vec3 b)
+{
+    return mk3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+// glm::clamp: min(max(x, lo), hi) with glm's ternary min / max (NaN passes through)
+VT_HD float gclamp(float x, float lo, float hi)
+{
+    float m = (x < lo) ? lo : x;
+    return (hi < m) ? hi : m;
+}
+VT_HD void acc3(vec3& a, vec3 b)
+{
+    a.x = a.x + b.x;
+    a.y = a.y + b.y;
+    a.z = a.z + b.z;
+}
+
+// mat4 (column-major) * (v, w), glm association
+VT_HD vec3 m4v3(const float* m, vec3 v, float w)
+{
+    return mk3((m[0] * v.x + m[4] * v.y) + (m[8] * v.z + m[12] * w),
+               (m[1] * v.x + m[5] * v.y) + (m[9] * v.z + m[13] * w),
+               (m[2] * v.x + m[6] * v.y) + (m[10] * v.z + m[14] * w));
+}
+// mat3 (column-major) * v
+VT_HD vec3 m3v3(const float* m, vec3 v)
+{
+    return mk3((m[0] * v.x + m[3] * v.y) + m[6] * v.z, (m[1] * v.x + m[4] * v.y) + m[7] * v.z,
+               (m[2] * v.x + m[5] * v.y) + m[8] * v.z);
+}
+// mat4 * mat4, glm: column j = ((A0*B[j][0] + A1*B[j][1]) + A2*B[j][2]) + A3*B[j][3]
+VT_HD void m4m4(const float* a, const float* b, float* out)
+{
+    for (int j = 0; j < 4; ++j)
+        for (int r = 0; r < 4; ++r) {
+            float s = a[0 + r] * b[4 * j + 0] + a[4 + r] * b[4 * j + 1];
+            s = s + a[8 + r] * b[4 * j + 2];
+            s = s + a[12 + r] * b[4 * j + 3];
+            out[4 * j + r] = s;
+        }
+}
+
+// arccos for the dihedral angle of the bending constraint.  The reference calls CUDA's
+// acosf; this is our own: the Maclaurin series of arcsin,
+//   arcsin(t) = t + sum_{n>=1} c_n t^(2n+1),  c_n = (2n)! / (4^n (n!)^2 (2n+1)),
+// truncated after n = 11 (|t| <= 1/2: truncation error < 1e-9 relative), with
+//   arccos(x) = 2 arcsin(sqrt((1-x)/2))          for x >=  1/2
+//             = pi - 2 arcsin(sqrt((1+x)/2))     for x <= -1/2
+//             = pi/2 - arcsin(x)                 otherwise.
+// Host and device evaluate the same operations, so they agree bit for bit.
+VT_HD float vt_asin_series(float t)
+{
+    const float c1 = 0.16666666666666666f, c2 = 0.075f, c3 = 0.044642857142857144f,
+                c4 = 0.030381944444444444f, c5 = 0.022372159090909092f,
+                c6 = 0.017352764423076924f, c7 = 0.01396484375f, c8 = 0.011551800896139705f,
+                c9 = 0.009761609529194078f, c10 = 0.008390335809616815f,
+                c11 = 0.0073125258735988454f;
+    float z = t * t;
+    float p = c11;
+    p = p * z + c10;
+    p = p * z + c9;
+    p = p * z + c8;
+    p = p * z + c7;
+    p = p * z + c6;
+    p = p * z + c5;
+    p = p * z + c4;
+    p = p * z + c3;
+    p = p * z + c2;
+    p = p * z + c1;
+    float r = z * p;
+    return t + t * r;
+}
+
+VT_HD float vt_acosf(float x)
+{
+    const float pio2_hi = 1.57079637050628662109375f;
+    const float pio2_lo = -4.37113900018624283e-8f;
+    if (x >= 0.5f) {
+        float s = sqrtf((1.0f - x) * 0.5f);
+        return 2.0f * vt_asin_series(s);
+    }
+    if (x <= -0.5f) {
+        float s = sqrtf((1.0f + x) * 0.5f);
+        return ((pio2_hi - vt_asin_series(s)) + pio2_lo) * 2.0f;
+    }
+    return (pio2_hi - vt_asin_series(x)) + pio2_lo;
+}

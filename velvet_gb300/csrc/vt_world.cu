@@ -1,0 +1,681 @@
+// vt_world.cu — builds the device state of one or more solver domains (CSR adjacency,
+// tile tables, hash buffers) and enqueues the launches of one frame.
+//
+// Schedule of one frame (Velvet/VtClothSolverGPU.hpp:56-111, with the fusions listed
+// in vt_kernels.cu):
+//   presdf_predict                           CollideSDF(x, frameDt) + Predict(substep 0)
+//   for each substep s:
+//     if self-collision and s % interleavedHash == 0:
+//        fill cell_start 0xff, hash_keys, radix sort, cell_ranges, cache_neighbors
+//     collide                                CollideParticles + ApplyDeltas + CollideSDF
+//     for each iteration: bend, solve        Stretch + Attach + Bending + ApplyDeltas
+//       (the last iteration's solve also runs Finalize and, except after the last
+//        substep, the next substep's Predict)
+//   normals
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "vt_host.h"
+#include "vt_math.cuh"
+
+namespace vt {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+const std::string& last_error() { return g_last_error; }
+
+vt_status cuda_fail(cudaError_t e, const char* what)
+{
+    set_error(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+    return e == cudaErrorMemoryAllocation ? VT_ERR_OUT_OF_MEMORY : VT_ERR_CUDA;
+}
+
+#define VT_CUDA(call, what)                                 \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what);  \
+    } while (0)
+
+static constexpr int kTile = 256;
+
+// ------------------------------------------------------------------ profiler
+namespace {
+struct Pending {
+    int stage;
+    cudaEvent_t e0, e1;
+};
+struct ProfilerState {
+    std::mutex mu;
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    std::vector<Pending> pending;
+    uint64_t launches[ST_COUNT] = {};
+    double ms[ST_COUNT] = {};
+};
+ProfilerState& prof()
+{
+    static ProfilerState* p = new ProfilerState();  // never destroyed: outlives static teardown
+    return *p;
+}
+cudaEvent_t take_event(ProfilerState& P)
+{
+    if (!P.pool.empty()) {
+        cudaEvent_t e = P.pool.back();
+        P.pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+// Folds finished event pairs into the totals; with `wait`, waits for all of them.
+void drain(ProfilerState& P, bool wait)
+{
+    std::vector<Pending> keep;
+    for (const Pending& q : P.pending) {
+        if (!wait && cudaEventQuery(q.e1) == cudaErrorNotReady) {
+            keep.push_back(q);
+            continue;
+        }
+        if (wait) cudaEventSynchronize(q.e1);
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, q.e0, q.e1) == cudaSuccess) {
+            P.ms[q.stage] += ms;
+            P.launches[q.stage] += 1;
+        }
+        P.pool.push_back(q.e0);
+        P.pool.push_back(q.e1);
+    }
+    cudaGetLastError();  // clear a not-ready status left by cudaEventQuery
+    P.pending.swap(keep);
+}
+}  // namespace
+
+const char* stage_name(int s)
+{
+    static const char* names[ST_COUNT] = {"presdf_predict", "hash_keys", "radix_sort", "cell_ranges",
+                                          "cache_neighbors", "collide", "bend", "solve", "finalize",
+                                          "normals", "batch_fused"};
+    return (s >= 0 && s < ST_COUNT) ? names[s] : "?";
+}
+
+bool profiler_on() { return prof().on; }
+
+StageScope::StageScope(int stage_, cudaStream_t st_) : stage(stage_), st(st_)
+{
+    ProfilerState& P = prof();
+    if (!P.on) return;
+    std::lock_guard<std::mutex> lock(P.mu);
+    e0 = take_event(P);
+    e1 = take_event(P);
+    cudaEventRecord(e0, st);
+}
+
+StageScope::~StageScope()
+{
+    if (!e0) return;
+    ProfilerState& P = prof();
+    std::lock_guard<std::mutex> lock(P.mu);
+    cudaEventRecord(e1, st);
+    P.pending.push_back(Pending{stage, e0, e1});
+    if (P.pending.size() > 4096) drain(P, false);
+}
+
+vt_status profiler_enable(bool on)
+{
+    ProfilerState& P = prof();
+    std::lock_guard<std::mutex> lock(P.mu);
+    P.on = on;
+    return VT_OK;
+}
+
+vt_status profiler_reset()
+{
+    ProfilerState& P = prof();
+    std::lock_guard<std::mutex> lock(P.mu);
+    drain(P, true);
+    for (int s = 0; s < ST_COUNT; ++s) {
+        P.ms[s] = 0;
+        P.launches[s] = 0;
+    }
+    return VT_OK;
+}
+
+vt_status profiler_read(vt_stage_time* out, uint32_t cap, uint32_t* count)
+{
+    ProfilerState& P = prof();
+    std::lock_guard<std::mutex> lock(P.mu);
+    drain(P, true);
+    uint32_t n = 0;
+    for (int s = 0; s < ST_COUNT; ++s) {
+        if (!P.launches[s]) continue;
+        if (out && n < cap) {
+            std::memset(&out[n], 0, sizeof(vt_stage_time));
+            std::strncpy(out[n].name, stage_name(s), sizeof(out[n].name) - 1);
+            out[n].launches = P.launches[s];
+            out[n].total_ms = P.ms[s];
+        }
+        ++n;
+    }
+    if (count) *count = n;
+    return VT_OK;
+}
+
+ColliderDev collider_to_device(const vt_sdf_collider& c)
+{
+    ColliderDev d{};
+    d.type = c.type;
+    d.px = c.position[0]; d.py = c.position[1]; d.pz = c.position[2];
+    d.sx = c.scale[0]; d.sy = c.scale[1]; d.sz = c.scale[2];
+    d.delta_time = c.delta_time;
+    std::memcpy(d.cur3, c.cur_transform, sizeof(d.cur3));
+    std::memcpy(d.inv, c.inv_cur_transform, sizeof(d.inv));
+    // VelocityAt: lastTransform * invCurTransform (glm mat4 product order)
+    m4m4(c.last_transform, c.inv_cur_transform, d.last_inv);
+    return d;
+}
+
+uint64_t HostSolver::device_bytes() const
+{
+    const uint64_t N = n(), B = nbend(), T = (uint64_t)table_size + 1;
+    uint64_t at = 0;
+    for (const AttachOp& a : at_ops) at += a.kind == 0 ? 1 : (uint64_t)a.p_count;
+    const uint64_t mn = (uint64_t)P.max_num_neighbors;
+    uint64_t b = 0;
+    b += N * 16 * 6;                       // x, v, x0, p[2], nrm
+    b += (N + 1) * 4 * 4;                  // st/at/bd/tn offsets
+    b += st_rest.size() * 2 * 8;           // stretch entries
+    b += at * 8;                           // attach entries
+    b += B * (16 + 4 + 64) + B * 4 * 4;    // bend idx, rest, corners, entries
+    b += tri.size() / 3 * (16 + 12);       // triangles + entries
+    b += N * 4 * 4 + (N / 4096 + 2) * 256 * 4;  // keys, vals, tmp, hist
+    b += T * 8 + mn * N * 4;               // cells, neighbours
+    b += (uint64_t)nslots() * 32 + colliders.size() * sizeof(ColliderDev);
+    return b + 64 * 256;                   // alignment slack
+}
+
+World::~World() { release(); }
+
+void World::release()
+{
+    if (gexec_) cudaGraphExecDestroy(gexec_);
+    if (cap_) cudaStreamDestroy(cap_);
+    if (arena_) cudaFree(arena_);
+    if (staging_) cudaFreeHost(staging_);
+    if (staged_) cudaEventDestroy(staged_);
+    gexec_ = nullptr;
+    cap_ = nullptr;
+    gkey_[0] = gkey_[1] = gkey_[2] = gkey_[3] = -1;
+    arena_ = nullptr;
+    staging_ = nullptr;
+    staged_ = nullptr;
+    d = DeviceArrays{};
+    hdom.clear();
+    hcol.clear();
+    hslots.clear();
+    built_ = false;
+    bytes = 0;
+}
+
+namespace {
+struct Arena {
+    size_t off = 0;
+    template <typename T>
+    size_t take(size_t count)
+    {
+        const size_t at = off;
+        off += (count * sizeof(T) + 255) & ~size_t(255);
+        return at;
+    }
+};
+
+void tiles_for(std::vector<Tile>& out, int dom, int begin, int count)
+{
+    for (int b = begin; b < begin + count; b += kTile) {
+        Tile t;
+        t.dom = dom;
+        t.begin = b;
+        t.end = std::min(begin + count, b + kTile);
+        t.pad_ = 0;
+        out.push_back(t);
+    }
+}
+
+// counting-sort style CSR: `rows` entries per row in the order items are pushed
+template <typename E>
+struct Csr {
+    std::vector<int32_t> off;
+    std::vector<E> ent;
+    std::vector<int32_t> cur;
+    void init(size_t rows) { off.assign(rows + 1, 0); }
+    void count(int32_t r) { off[r + 1]++; }
+    void finish_counts()
+    {
+        for (size_t r = 1; r < off.size(); ++r) off[r] += off[r - 1];
+        ent.resize(off.back());
+        cur.assign(off.begin(), off.end() - 1);
+    }
+    void put(int32_t r, const E& e) { ent[cur[r]++] = e; }
+};
+}  // namespace
+
+vt_status World::build(const std::vector<const HostSolver*>& S)
+{
+    release();
+    n_domains = (int32_t)S.size();
+    int64_t N = 0, B = 0, SL = 0, C = 0, G = 0, TR = 0, TK = 0, NW = 0;
+    for (const HostSolver* h : S) {
+        N += h->n();
+        B += h->nbend();
+        SL += h->nslots();
+        C += (int64_t)h->colliders.size();
+        TR += (int64_t)h->tri.size() / 3;
+        TK += (int64_t)h->table_size + 1;
+        NW += (int64_t)h->P.max_num_neighbors * h->n();
+        for (const AttachOp& a : h->at_ops) G += a.kind == 1;
+    }
+    if (N > INT32_MAX / 2 || TK > INT32_MAX / 2 || NW > INT32_MAX) {
+        set_error("world too large for 32-bit indices");
+        return VT_ERR_CAPACITY;
+    }
+    n_particles = (int32_t)N;
+    n_bends = (int32_t)B;
+    n_slots = (int32_t)SL;
+    n_cols = (int32_t)C;
+    total_keys = (int32_t)TK;
+    nbr_words = (int32_t)NW;
+
+    // ---- host images
+    std::vector<float4> hx(N), hv(N), hx0(N), hp(N);
+    std::vector<float4> hslot(SL), hslot0(SL);
+    std::vector<LraGroup> hlra;
+    std::vector<uint4> hbd(B);
+    std::vector<float> hbr(B);
+    std::vector<uint4> htri(TR);
+    Csr<int2> st;
+    Csr<int2> at;
+    Csr<int32_t> bd;
+    Csr<int32_t> tn;
+    st.init(N);
+    at.init(N);
+    bd.init(N);
+    tn.init(N);
+    std::vector<Tile> pt, bt;
+    hdom.assign(n_domains, DomainParams{});
+    hcol.clear();
+
+    int32_t pb = 0, bb = 0, sb = 0, tb = 0, tkb = 0, nwb = 0, gb = 0, cb = 0;
+    // pass 1: counts
+    {
+        int32_t p0 = 0, b0 = 0, t0 = 0;
+        for (const HostSolver* h : S) {
+            for (size_t c = 0; c < h->st_rest.size(); ++c) {
+                st.count(p0 + h->st_idx[2 * c]);
+                st.count(p0 + h->st_idx[2 * c + 1]);
+            }
+            for (const AttachOp& a : h->at_ops) {
+                if (a.kind == 0) at.count(p0 + a.pid);
+                else
+                    for (int32_t i = 0; i < a.p_count; ++i) at.count(p0 + a.p_begin + i);
+            }
+            for (size_t k = 0; k < h->bd_idx.size(); ++k) bd.count(p0 + (int32_t)h->bd_idx[k]);
+            for (size_t k = 0; k < h->tri.size() / 3 * 3; ++k) tn.count(p0 + (int32_t)h->tri[k]);
+            p0 += (int32_t)h->n();
+            b0 += (int32_t)h->nbend();
+            t0 += (int32_t)(h->tri.size() / 3);
+        }
+        (void)b0;
+        (void)t0;
+    }
+    st.finish_counts();
+    at.finish_counts();
+    bd.finish_counts();
+    tn.finish_counts();
+
+    // pass 2: fill
+    for (int32_t k = 0; k < n_domains; ++k) {
+        const HostSolver& h = *S[k];
+        const int32_t n = (int32_t)h.n();
+        for (int32_t i = 0; i < n; ++i) {
+            const float w = h.w[i];
+            hx[pb + i] = make_float4(h.x[3 * i], h.x[3 * i + 1], h.x[3 * i + 2], w);
+            hv[pb + i] = make_float4(h.v[3 * i], h.v[3 * i + 1], h.v[3 * i + 2], 0.0f);
+            hx0[pb + i] = make_float4(h.x0[3 * i], h.x0[3 * i + 1], h.x0[3 * i + 2], 0.0f);
+            hp[pb + i] = make_float4(0, 0, 0, w);
+        }
+        for (uint32_t s = 0; s < h.nslots(); ++s) {
+            hslot[sb + s] = make_float4(h.slots[3 * s], h.slots[3 * s + 1], h.slots[3 * s + 2], 0.0f);
+            hslot0[sb + s] = make_float4(h.slots0[3 * s], h.slots0[3 * s + 1], h.slots0[3 * s + 2], 0.0f);
+        }
+        for (size_t c = 0; c < h.st_rest.size(); ++c) {
+            const int32_t a = pb + h.st_idx[2 * c], b = pb + h.st_idx[2 * c + 1];
+            int32_t rb;
+            std::memcpy(&rb, &h.st_rest[c], 4);
+            st.put(a, make_int2(b, rb));
+            st.put(b, make_int2(a, rb));
+        }
+        for (const AttachOp& a : h.at_ops) {
+            if (a.kind == 0) {
+                int32_t db;
+                std::memcpy(&db, &a.dist, 4);
+                at.put(pb + a.pid, make_int2(sb + a.slot, db));
+            } else {
+                LraGroup g;
+                g.slot_begin = sb + a.slot_begin;
+                g.slot_count = a.slot_count;
+                g.p_begin = pb + a.p_begin;
+                g.p_count = a.p_count;
+                hlra.push_back(g);
+                const int32_t gid = gb++;
+                for (int32_t i = 0; i < a.p_count; ++i) at.put(pb + a.p_begin + i, make_int2(-(gid + 1), 0));
+            }
+        }
+        for (uint32_t c = 0; c < h.nbend(); ++c) {
+            const uint32_t* q = &h.bd_idx[4 * c];
+            hbd[bb + c] = make_uint4(pb + q[0], pb + q[1], pb + q[2], pb + q[3]);
+            hbr[bb + c] = h.bd_rest[c];
+            for (int j = 0; j < 4; ++j) bd.put(pb + (int32_t)q[j], 4 * (bb + (int32_t)c) + j);
+        }
+        const int32_t ntri = (int32_t)(h.tri.size() / 3);
+        for (int32_t t = 0; t < ntri; ++t) {
+            const uint32_t* q = &h.tri[3 * t];
+            htri[tb + t] = make_uint4(pb + q[0], pb + q[1], pb + q[2], 0);
+            for (int j = 0; j < 3; ++j) tn.put(pb + (int32_t)q[j], tb + t);
+        }
+        for (const vt_sdf_collider& c : h.colliders) hcol.push_back(collider_to_device(c));
+
+        DomainParams& D = hdom[k];
+        D.p_begin = pb;
+        D.p_count = n;
+        D.col_begin = cb;
+        D.col_count = (int32_t)h.colliders.size();
+        D.table_base = tkb;
+        D.table_size = h.table_size;
+        D.nbr_base = nwb;
+        D.max_nbr = h.P.max_num_neighbors;
+        D.cell_spacing = h.cell_spacing;
+        D.cell_spacing2 = h.cell_spacing * h.cell_spacing;
+        tiles_for(pt, k, pb, n);
+        tiles_for(bt, k, bb, (int32_t)h.nbend());
+
+        pb += n;
+        bb += (int32_t)h.nbend();
+        sb += (int32_t)h.nslots();
+        tb += ntri;
+        tkb += h.table_size + 1;
+        nwb += h.P.max_num_neighbors * n;
+        cb += (int32_t)h.colliders.size();
+    }
+    n_ptiles = (int32_t)pt.size();
+    n_btiles = (int32_t)bt.size();
+    hslots = hslot;
+
+    // ---- device arena
+    Arena A;
+    const size_t o_x = A.take<float4>(N), o_v = A.take<float4>(N), o_x0 = A.take<float4>(N);
+    const size_t o_p0 = A.take<float4>(N), o_p1 = A.take<float4>(N), o_nrm = A.take<float4>(N);
+    const size_t o_sto = A.take<int32_t>(N + 1), o_ste = A.take<int2>(st.ent.size());
+    const size_t o_ato = A.take<int32_t>(N + 1), o_ate = A.take<int2>(at.ent.size());
+    const size_t o_lra = A.take<LraGroup>(hlra.size());
+    const size_t o_sl = A.take<float4>(SL), o_sl0 = A.take<float4>(SL);
+    const size_t o_bdi = A.take<uint4>(B), o_bdr = A.take<float>(B), o_bdc = A.take<float4>(4 * B);
+    const size_t o_bdo = A.take<int32_t>(N + 1), o_bde = A.take<int32_t>(bd.ent.size());
+    const size_t o_tri = A.take<uint4>(TR), o_tno = A.take<int32_t>(N + 1), o_tne = A.take<int32_t>(tn.ent.size());
+    const size_t o_k = A.take<uint32_t>(N), o_vl = A.take<uint32_t>(N);
+    const size_t o_kt = A.take<uint32_t>(N), o_vt = A.take<uint32_t>(N);
+    const size_t o_h = A.take<uint32_t>(radix_hist_words((int32_t)N)), o_dt = A.take<uint32_t>(256);
+    const size_t o_cs = A.take<uint32_t>(TK), o_ce = A.take<uint32_t>(TK), o_nb = A.take<uint32_t>(NW);
+    const size_t o_dom = A.take<DomainParams>(n_domains), o_col = A.take<ColliderDev>(C);
+    const size_t o_pt = A.take<Tile>(pt.size()), o_bt = A.take<Tile>(bt.size());
+    const size_t o_st = A.take<int32_t>(1 + n_domains);
+    bytes = A.off;
+    VT_CUDA(cudaMalloc(&arena_, A.off), "cudaMalloc(world)");
+    char* base = (char*)arena_;
+#define AT(T, o) reinterpret_cast<T*>(base + (o))
+    d.x = AT(float4, o_x); d.v = AT(float4, o_v); d.x0 = AT(float4, o_x0);
+    d.p[0] = AT(float4, o_p0); d.p[1] = AT(float4, o_p1); d.nrm = AT(float4, o_nrm);
+    d.st_off = AT(int32_t, o_sto); d.st_ent = AT(int2, o_ste);
+    d.at_off = AT(int32_t, o_ato); d.at_ent = AT(int2, o_ate); d.lra = AT(LraGroup, o_lra);
+    d.slots = AT(float4, o_sl); d.slots0 = AT(float4, o_sl0);
+    d.bd_idx = AT(uint4, o_bdi); d.bd_rest = AT(float, o_bdr); d.bd_corr = AT(float4, o_bdc);
+    d.bd_off = AT(int32_t, o_bdo); d.bd_ent = AT(int32_t, o_bde);
+    d.tri = AT(uint4, o_tri); d.tn_off = AT(int32_t, o_tno); d.tn_ent = AT(int32_t, o_tne);
+    d.keys = AT(uint32_t, o_k); d.vals = AT(uint32_t, o_vl);
+    d.keys_tmp = AT(uint32_t, o_kt); d.vals_tmp = AT(uint32_t, o_vt);
+    d.hist = AT(uint32_t, o_h); d.digit_tot = AT(uint32_t, o_dt);
+    d.cell_start = AT(uint32_t, o_cs); d.cell_end = AT(uint32_t, o_ce); d.nbr = AT(uint32_t, o_nb);
+    d.dom = AT(DomainParams, o_dom); d.col = AT(ColliderDev, o_col);
+    d.ptiles = AT(Tile, o_pt); d.btiles = AT(Tile, o_bt); d.status = AT(int32_t, o_st);
+#undef AT
+    auto up = [](void* dst, const void* src, size_t bytes_) -> cudaError_t {
+        return bytes_ ? cudaMemcpy(dst, src, bytes_, cudaMemcpyHostToDevice) : cudaSuccess;
+    };
+    VT_CUDA(up(d.x, hx.data(), N * 16), "upload x");
+    VT_CUDA(up(d.v, hv.data(), N * 16), "upload v");
+    VT_CUDA(up(d.x0, hx0.data(), N * 16), "upload x0");
+    VT_CUDA(up(d.p[0], hp.data(), N * 16), "upload p");
+    VT_CUDA(up(d.p[1], hp.data(), N * 16), "upload p");
+    VT_CUDA(cudaMemset(d.nrm, 0, N * 16), "memset nrm");
+    VT_CUDA(up(d.st_off, st.off.data(), (N + 1) * 4), "upload st_off");
+    VT_CUDA(up(d.st_ent, st.ent.data(), st.ent.size() * 8), "upload st_ent");
+    VT_CUDA(up(d.at_off, at.off.data(), (N + 1) * 4), "upload at_off");
+    VT_CUDA(up(d.at_ent, at.ent.data(), at.ent.size() * 8), "upload at_ent");
+    VT_CUDA(up(d.lra, hlra.data(), hlra.size() * sizeof(LraGroup)), "upload lra");
+    VT_CUDA(up(d.slots, hslot.data(), SL * 16), "upload slots");
+    VT_CUDA(up(d.slots0, hslot0.data(), SL * 16), "upload slots0");
+    VT_CUDA(up(d.bd_idx, hbd.data(), B * 16), "upload bd_idx");
+    VT_CUDA(up(d.bd_rest, hbr.data(), B * 4), "upload bd_rest");
+    VT_CUDA(up(d.bd_off, bd.off.data(), (N + 1) * 4), "upload bd_off");
+    VT_CUDA(up(d.bd_ent, bd.ent.data(), bd.ent.size() * 4), "upload bd_ent");
+    VT_CUDA(up(d.tri, htri.data(), TR * 16), "upload tri");
+    VT_CUDA(up(d.tn_off, tn.off.data(), (N + 1) * 4), "upload tn_off");
+    VT_CUDA(up(d.tn_ent, tn.ent.data(), tn.ent.size() * 4), "upload tn_ent");
+    VT_CUDA(cudaMemset(d.cell_start, 0xff, (size_t)TK * 4), "memset cell_start");
+    VT_CUDA(cudaMemset(d.cell_end, 0, (size_t)TK * 4), "memset cell_end");
+    VT_CUDA(cudaMemset(d.nbr, 0xff, (size_t)NW * 4), "memset nbr");
+    VT_CUDA(up(d.ptiles, pt.data(), pt.size() * sizeof(Tile)), "upload ptiles");
+    VT_CUDA(up(d.btiles, bt.data(), bt.size() * sizeof(Tile)), "upload btiles");
+    VT_CUDA(cudaMemset(d.status, 0, (1 + n_domains) * 4), "memset status");
+
+    staging_bytes_ = sizeof(DomainParams) * n_domains + sizeof(ColliderDev) * C + 16 * SL + 64;
+    VT_CUDA(cudaMallocHost(&staging_, staging_bytes_), "cudaMallocHost(staging)");
+    VT_CUDA(cudaEventCreateWithFlags(&staged_, cudaEventDisableTiming), "cudaEventCreate");
+    VT_CUDA(cudaDeviceSynchronize(), "world upload");
+    cols_dirty_ = true;
+    slots_dirty_ = true;
+    pcur = 0;
+    built_ = true;
+    return VT_OK;
+}
+
+void World::set_frame(int k, const HostSolver& h, const FrameArgs& a)
+{
+    DomainParams& D = hdom[k];
+    const vt_params& P = h.P;
+    D.diameter = a.diameter;
+    D.diameter2 = a.diameter * a.diameter;
+    D.gx = P.gravity[0];
+    D.gy = P.gravity[1];
+    D.gz = P.gravity[2];
+    D.dt_frame = a.frame_dt;
+    D.dt_sub = a.frame_dt / (float)a.substeps;
+    D.relax = a.relax;
+    D.friction = a.friction;
+    D.margin = a.margin;
+    D.max_speed = P.max_speed;
+    D.damping = P.damping;
+    D.lrs = P.long_range_stretchiness;
+    D.bend_compliance = P.bend_compliance;
+    D.self_collision = P.enable_self_collision ? 1 : 0;
+}
+
+vt_status World::set_colliders(int k, const std::vector<vt_sdf_collider>& c)
+{
+    DomainParams& D = hdom[k];
+    if ((int32_t)c.size() != D.col_count) {
+        set_error("collider count of a built world cannot change; rebuild");
+        return VT_ERR_STATE;
+    }
+    for (size_t j = 0; j < c.size(); ++j) hcol[D.col_begin + j] = collider_to_device(c[j]);
+    cols_dirty_ = true;
+    return VT_OK;
+}
+
+vt_status World::set_slot(int k, int32_t slot, const float xyz[3])
+{
+    (void)k;
+    if (slot < 0 || slot >= n_slots) return VT_ERR_INVALID_ARGUMENT;
+    hslots[slot] = make_float4(xyz[0], xyz[1], xyz[2], 0.0f);
+    slots_dirty_ = true;
+    return VT_OK;
+}
+
+int64_t World::launches_per_frame(int32_t S, int32_t It, int32_t ih, bool self, bool bends,
+                                  int32_t n, int32_t tk)
+{
+    int64_t L = 1 + 1;  // presdf_predict + normals
+    int bits = 0;
+    while ((1ll << bits) < (int64_t)tk) ++bits;
+    const int passes = (n > 1 && bits > 0) ? (bits + 7) / 8 : 0;
+    for (int s = 0; s < S; ++s) {
+        if (self && s % ih == 0) L += 3 + 3 * passes;  // keys, ranges, cache + sort
+        L += 1;                                         // collide
+        L += (int64_t)It * (bends ? 2 : 1);
+        if (It == 0) L += 1;
+    }
+    return L;
+}
+
+vt_status World::simulate(const FrameArgs& a, int32_t ih, bool any_self, cudaStream_t st,
+                          bool use_graph)
+{
+    if (!built_) return VT_ERR_STATE;
+    if (n_particles == 0) return VT_OK;
+    vt_status r = upload_frame(st);
+    if (r != VT_OK) return r;
+    if (!use_graph || profiler_on()) return enqueue_frame(a, ih, any_self, st);
+    const int32_t key[4] = {a.substeps, a.iterations, ih, any_self ? 1 : 0};
+    if (!gexec_ || std::memcmp(key, gkey_, sizeof(key)) != 0) {
+        if (gexec_) {
+            VT_CUDA(cudaGraphExecDestroy(gexec_), "cudaGraphExecDestroy");
+            gexec_ = nullptr;
+        }
+        if (!cap_) VT_CUDA(cudaStreamCreateWithFlags(&cap_, cudaStreamNonBlocking), "cudaStreamCreate");
+        const uint64_t before = launches;
+        VT_CUDA(cudaStreamBeginCapture(cap_, cudaStreamCaptureModeThreadLocal), "begin capture");
+        vt_status er = enqueue_frame(a, ih, any_self, cap_);
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(cap_, &g);
+        if (er != VT_OK) {
+            if (g) cudaGraphDestroy(g);
+            return er;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ce, "end capture");
+        ce = cudaGraphInstantiate(&gexec_, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            gexec_ = nullptr;
+            return cuda_fail(ce, "cudaGraphInstantiate");
+        }
+        glaunches_ = launches - before;
+        launches = before;
+        gpcur_ = pcur;
+        std::memcpy(gkey_, key, sizeof(key));
+    }
+    VT_CUDA(cudaGraphLaunch(gexec_, st), "cudaGraphLaunch");
+    launches += glaunches_;
+    pcur = gpcur_;
+    return VT_OK;
+}
+
+vt_status World::upload_frame(cudaStream_t st)
+{
+    // stage small per-frame uploads (guarded: the previous copy must have left staging)
+    VT_CUDA(cudaEventSynchronize(staged_), "staging event");
+    char* s = (char*)staging_;
+    const size_t dom_b = sizeof(DomainParams) * n_domains;
+    std::memcpy(s, hdom.data(), dom_b);
+    VT_CUDA(cudaMemcpyAsync(d.dom, s, dom_b, cudaMemcpyHostToDevice, st), "upload params");
+    size_t off = dom_b;
+    if (cols_dirty_ && n_cols) {
+        const size_t cb = sizeof(ColliderDev) * n_cols;
+        std::memcpy(s + off, hcol.data(), cb);
+        VT_CUDA(cudaMemcpyAsync(d.col, s + off, cb, cudaMemcpyHostToDevice, st), "upload colliders");
+        off += cb;
+    }
+    if (slots_dirty_ && n_slots) {
+        const size_t sb = 16 * (size_t)n_slots;
+        std::memcpy(s + off, hslots.data(), sb);
+        VT_CUDA(cudaMemcpyAsync(d.slots, s + off, sb, cudaMemcpyHostToDevice, st), "upload slots");
+    }
+    VT_CUDA(cudaEventRecord(staged_, st), "staging record");
+    cols_dirty_ = slots_dirty_ = false;
+    return VT_OK;
+}
+
+vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cudaStream_t st)
+{
+    Launch L{&d, n_ptiles, n_btiles, n_particles, st};
+    int pc = 0;
+    int bits = 0;
+    while ((1ll << bits) < (int64_t)total_keys) ++bits;
+    const int sort_passes = (n_particles > 1 && bits > 0) ? (bits + 7) / 8 : 0;
+    const uint64_t pk = n_ptiles ? 1 : 0, bk = n_btiles ? 1 : 0;
+#define VT_STAGE(stage, call, what, count)          \
+    do {                                            \
+        StageScope scope_(stage, st);               \
+        VT_CUDA(call, what);                        \
+        launches += (count);                        \
+    } while (0)
+    VT_STAGE(ST_PRESDF_PREDICT, launch_presdf_predict(L, pc), "presdf_predict", pk);
+    for (int sub = 0; sub < a.substeps; ++sub) {
+        if (any_self && sub % ih == 0) {
+            VT_CUDA(cudaMemsetAsync(d.cell_start, 0xff, (size_t)total_keys * 4, st), "memset cells");
+            VT_STAGE(ST_HASH_KEYS, launch_hash_keys(L, pc), "hash_keys", pk);
+            VT_STAGE(ST_RADIX_SORT,
+                     radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot,
+                                      n_particles, bits, st),
+                     "radix_sort", 3 * (uint64_t)sort_passes);
+            VT_STAGE(ST_CELL_RANGES, launch_cell_ranges(d.keys, n_particles, d.cell_start, d.cell_end, st),
+                     "cell_ranges", 1);
+            VT_STAGE(ST_CACHE_NEIGHBORS, launch_cache_neighbors(L, pc), "cache_neighbors", pk);
+        }
+        VT_STAGE(ST_COLLIDE, launch_collide(L, pc, 1 - pc), "collide", pk);
+        pc = 1 - pc;
+        const bool last_sub = sub == a.substeps - 1;
+        for (int it = 0; it < a.iterations; ++it) {
+            if (n_btiles) VT_STAGE(ST_BEND, launch_bend(L, pc), "bend", bk);
+            const int mode = it < a.iterations - 1 ? SOLVE_PLAIN
+                                                   : (last_sub ? SOLVE_FINALIZE : SOLVE_FINALIZE_PREDICT);
+            VT_STAGE(ST_SOLVE, launch_solve(L, pc, 1 - pc, mode), "solve", pk);
+            pc = 1 - pc;
+        }
+        if (a.iterations == 0)
+            VT_STAGE(ST_FINALIZE, launch_finalize(L, pc, last_sub ? 0 : 1), "finalize", pk);
+    }
+    VT_STAGE(ST_NORMALS, launch_normals(L), "normals", pk);
+#undef VT_STAGE
+    pcur = pc;
+    return VT_OK;
+}
+
+vt_status World::read_status(std::vector<int32_t>& flags, cudaStream_t st)
+{
+    flags.assign(1 + n_domains, 0);
+    if (!built_) return VT_OK;
+    VT_CUDA(cudaMemcpyAsync(flags.data(), d.status, flags.size() * 4, cudaMemcpyDeviceToHost, st),
+            "read status");
+    VT_CUDA(cudaStreamSynchronize(st), "sync status");
+    return VT_OK;
+}
+
+vt_status World::clear_status(cudaStream_t st)
+{
+    if (!built_) return VT_OK;
+    VT_CUDA(cudaMemsetAsync(d.status, 0, (1 + n_domains) * 4, st), "clear status");
+    return VT_OK;
+}
+
+}  // namespace vt

@@ -1,0 +1,133 @@
+// vt_world.h — device-side layout of one or more independent cloth-solver domains.
+//
+// A domain is everything one VtClothSolverGPU instance owns (Velvet/VtClothSolverGPU.hpp:
+// 207-237): a particle range, its constraints, colliders, attach slots, parameter block
+// and spatial hash.  The plain solver is one domain holding all of its cloths (merged,
+// as the reference merges them: one hash, one diameter, cloths collide with each
+// other).  The batched and served forms hold many domains, one per independent cloth,
+// and advance them all with the same launches: every kernel reads a tile table that
+// maps each thread block to (domain, first item, end item), so a block never spans two
+// domains and per-domain parameters are loaded once per block.
+//
+// HBM layout (all arrays concatenated over domains, in domain order):
+//   particles   x, v, x0      float4 (xyz, w = inverse mass for x; 0 otherwise)
+//               p[2]          float4 ping-pong predicted positions (w = inverse mass)
+//               nrm           float4 normals
+//   stretch     st_off[N+1]   CSR offsets per particle, st_ent int2 (other, rest bits),
+//                             each particle's entries in constraint order
+//   attach      at_off[N+1]   CSR offsets, at_ent int2 (slot | -(group+1), dist bits)
+//   bending     bd_idx uint4, bd_rest float per constraint; bd_corr float4 per
+//               (constraint, corner): correction + fired flag; bd_off/bd_ent CSR of
+//               corner slots per particle in constraint order
+//   normals     tn_off/tn_ent CSR of triangles per vertex; tri uint4 per triangle
+//   hash        keys/vals (sorted pairs), cell_start (sum of (T_d + 1)), cell_end,
+//               neighbours (max_nbr * n_d per domain, column-major inside a domain)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/velvet_gb300.h"
+
+namespace vt {
+
+// Per-domain parameters, rewritten on the device before every frame.
+struct DomainParams {
+    int32_t p_begin, p_count;      // particle range
+    int32_t col_begin, col_count;  // colliders
+    int32_t table_base, table_size; // hash cells [table_base, table_base + table_size)
+    int32_t nbr_base, max_nbr;     // neighbour block of this domain
+    float cell_spacing, cell_spacing2, diameter, diameter2;
+    float gx, gy, gz;
+    float dt_frame, dt_sub;
+    float relax, friction, margin, max_speed, damping, lrs, bend_compliance;
+    int32_t self_collision;
+    int32_t pad_[3];
+};
+
+// One collider on the device: the reference's SDFCollider with VelocityAt's matrix
+// product lastTransform * invCurTransform precomputed (same arithmetic, once per frame).
+struct ColliderDev {
+    int32_t type;
+    float px, py, pz;
+    float sx, sy, sz;
+    float delta_time;
+    float cur3[9];
+    float inv[16];
+    float last_inv[16];
+    float pad_[1];
+};
+
+// LRA group: every particle of [p_begin, p_begin + p_count) attached to each slot of
+// [slot_begin, slot_begin + slot_count), rest distance |slot0 - x0| recomputed.
+struct LraGroup {
+    int32_t slot_begin, slot_count, p_begin, p_count;
+};
+
+// Block tile: (domain, begin, end) of the items one thread block processes.
+struct Tile {
+    int32_t dom, begin, end, pad_;
+};
+
+struct DeviceArrays {
+    // particles
+    float4 *x = nullptr, *v = nullptr, *x0 = nullptr, *p[2] = {nullptr, nullptr}, *nrm = nullptr;
+    // constraints
+    int32_t *st_off = nullptr; int2* st_ent = nullptr;
+    int32_t *at_off = nullptr; int2* at_ent = nullptr;
+    LraGroup* lra = nullptr;
+    float4 *slots = nullptr, *slots0 = nullptr;
+    uint4* bd_idx = nullptr; float* bd_rest = nullptr; float4* bd_corr = nullptr;
+    int32_t *bd_off = nullptr, *bd_ent = nullptr;
+    uint4* tri = nullptr; int32_t *tn_off = nullptr, *tn_ent = nullptr;
+    // hash
+    uint32_t *keys = nullptr, *vals = nullptr, *keys_tmp = nullptr, *vals_tmp = nullptr;
+    uint32_t *hist = nullptr, *digit_tot = nullptr;
+    uint32_t *cell_start = nullptr, *cell_end = nullptr, *nbr = nullptr;
+    // tables
+    DomainParams* dom = nullptr;
+    ColliderDev* col = nullptr;
+    Tile *ptiles = nullptr, *btiles = nullptr;
+    int32_t* status = nullptr;  // device-side fault flag
+};
+
+// ------------------------------------------------------------------ kernel launchers
+// (vt_kernels.cu).  All enqueue on `st` and return the launch error, if any.
+struct Launch {
+    const DeviceArrays* d;
+    int32_t n_ptiles, n_btiles;
+    int32_t n_particles;
+    cudaStream_t st;
+};
+
+cudaError_t launch_presdf_predict(const Launch& L, int pcur);
+cudaError_t launch_collide(const Launch& L, int pin, int pout);
+cudaError_t launch_bend(const Launch& L, int pin);
+cudaError_t launch_solve(const Launch& L, int pin, int pout, int final_mode);
+cudaError_t launch_finalize(const Launch& L, int pcur, int predict_next);
+cudaError_t launch_normals(const Launch& L);
+
+// final_mode of launch_solve / predict_next of launch_finalize
+enum { SOLVE_PLAIN = 0, SOLVE_FINALIZE = 1, SOLVE_FINALIZE_PREDICT = 2 };
+
+// Spatial hash (vt_hash.cu)
+cudaError_t launch_hash_keys(const Launch& L, int pin);
+// Stable LSD radix sort of (keys, vals) pairs by the low `bits` bits of the keys;
+// result lands in keys / vals.  Scratch: keys_tmp, vals_tmp, hist, digit_tot.
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
+                             uint32_t* vals_tmp, uint32_t* hist, uint32_t* digit_tot,
+                             int32_t n, int32_t bits, cudaStream_t st);
+size_t radix_hist_words(int32_t n);  // size of `hist` for n items
+cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_start,
+                               uint32_t* cell_end, cudaStream_t st);
+cudaError_t launch_cache_neighbors(const Launch& L, int pin);
+// HashObjects on float3 caller buffers (vt_hash_objects); scratch supplied by the caller:
+// keys_tmp / vals_tmp num_objects words each, hist radix_hist_words(num_objects),
+// digit_tot 256 words.
+cudaError_t hash_objects_f3(uint32_t* phash, uint32_t* pindex, uint32_t* cell_start,
+                            uint32_t* cell_end, uint32_t* neighbors, const float* positions,
+                            const float* original, const vt_hash_params& hp,
+                            uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* hist,
+                            uint32_t* digit_tot, cudaStream_t st);
+
+}  // namespace vt
