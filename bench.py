@@ -236,7 +236,7 @@ def run_reference(args) -> None:
 
 
 # ---------------------------------------------------------------------------- GPU arm
-def build_plain_solvers(wl):
+def build_plain_solvers(wl, graphs=True):
     import velvet_gb300 as vg
     from velvet_gb300 import workloads as W
 
@@ -244,8 +244,22 @@ def build_plain_solvers(wl):
     for spec in wl.cloths:
         s = vg.ClothSolver()
         W.build_plain(spec, s)
+        vg._abi.check(vg.lib().vt_solver_use_graphs(s.handle, 1 if graphs else 0), "vt_solver_use_graphs")
         solvers.append((s, spec, spec.particle_diameter()))
     return solvers
+
+
+def build_batch(wl):
+    import velvet_gb300 as vg
+    from velvet_gb300 import workloads as W
+
+    batch = vg.BatchSolver()
+    for spec in wl.cloths:
+        s = vg.ClothSolver()
+        W.build_plain(spec, s)
+        batch.add(s)
+        s.close()
+    return batch
 
 
 def plain_frame(wl, solvers, frame, stream, upload_colliders):
@@ -254,6 +268,14 @@ def plain_frame(wl, solvers, frame, stream, upload_colliders):
             s.update_colliders(spec.colliders(frame))
         s.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
                    wl.collision_margin, d, stream)
+
+
+def batch_frame(wl, batch, frame, stream, upload_colliders):
+    if upload_colliders:
+        for k, spec in enumerate(wl.cloths):
+            batch.update_colliders(k, spec.colliders(frame))
+    batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                   wl.collision_margin, None, stream)
 
 
 def launch_total(solvers) -> int:
@@ -275,13 +297,20 @@ def profile_frames(args) -> None:
     import torch
 
     wl = workload(args.workload, args.seed)
-    solvers = build_plain_solvers(wl)
-    for f in range(args.profile_frames):
-        plain_frame(wl, solvers, f, None, upload_colliders=False)
+    if args.form == "plain":
+        solvers = build_plain_solvers(wl, graphs=False)
+        for f in range(args.profile_frames):
+            plain_frame(wl, solvers, f, None, upload_colliders=False)
+        for s, _, _ in solvers:
+            s.sync()
+    else:
+        batch = build_batch(wl)
+        batch.use_graphs(False)
+        for f in range(args.profile_frames):
+            batch_frame(wl, batch, f, None, upload_colliders=False)
+        batch.sync()
     torch.cuda.synchronize()
-    for s, _, _ in solvers:
-        s.sync()
-    print(json.dumps({"profiled_frames": args.profile_frames, "workload": wl.name,
+    print(json.dumps({"profiled_frames": args.profile_frames, "workload": wl.name, "form": args.form,
                       "particles": wl.num_particles}))
 
 
@@ -304,6 +333,11 @@ def timed_device(step_fn, steps, warmup, stream, dist_sync):
     return ev[0].elapsed_time(ev[steps]), per
 
 
+def pct(v, q):
+    s = sorted(v)
+    return s[min(len(s) - 1, int(q * len(s)))]
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,8 +345,11 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="batched")
+    ap.add_argument("--form", choices=["batched", "plain"], default="batched",
+                    help="form run by --profile-frames")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain solver")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only run this many frames of the workload and exit (for ncu captures)")
     args = ap.parse_args()
@@ -341,101 +378,117 @@ def main() -> None:
         if dist is not None:
             dist.barrier()
 
+    def max_over_ranks(x: float) -> float:
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
     wl = workload(args.workload, args.seed)
     stream = torch.cuda.Stream()
     pits = pits_per_frame(wl)
-
-    # ---- plain drop-in solver, one cloth at a time (the current headline form)
-    solvers = build_plain_solvers(wl)
-    step = lambda f: plain_frame(wl, solvers, f, stream, upload_colliders=False)  # noqa: E731
+    n_tot = wl.num_particles
     props = torch.cuda.get_device_properties(local)
     bus = getattr(props, "pci_bus_id", None)
     pci = None
     if bus is not None:
         pci = f"{getattr(props, 'pci_domain_id', 0):08x}:{bus:02x}:{getattr(props, 'pci_device_id', 0):02x}.0"
-    launches0 = launch_total(solvers)
-    clocks = ClockSampler(local, pci)
-    total_ms, per = timed_device(step, args.steps, args.warmup, stream, dist_sync)
-    clock_info = clocks.stop()
-    launches = launch_total(solvers) - launches0
-    # launches counted cover warm-up too; keep only the timed steps' share
-    launches_timed = int(round(launches * args.steps / (args.steps + args.warmup)))
 
-    elapsed = torch.tensor([total_ms], device="cuda")
-    if dist is not None:
-        dist.all_reduce(elapsed, op=dist.ReduceOp.MAX)
-    total_ms = float(elapsed.item())
+    # ---- batched form: every cloth advanced by one CUDA graph launch per frame
+    batch = build_batch(wl)
+    bstep = lambda f: batch_frame(wl, batch, f, stream, upload_colliders=False)  # noqa: E731
+    for f in range(args.warmup):
+        bstep(f)
+    torch.cuda.synchronize()
+    l0 = batch.launch_count()
+    clocks = ClockSampler(local, pci)
+    total_ms, per = timed_device(bstep, args.steps, 0, stream, dist_sync)
+    clock_info = clocks.stop()
+    launches_timed = batch.launch_count() - l0
+    total_ms = max_over_ranks(total_ms)
     value = pits * args.steps * world / (total_ms / 1000.0)
 
-    # ---- roofline of the dominant stage: one Jacobi iteration (bend + solve)
+    # ---- roofline of the dominant stage: one Jacobi iteration (bend + solve), events
+    # around each launch on the launching stream (graphs off while profiling)
     _abi.profiler_reset()
     _abi.profiler_enable(True)
     for k in range(2):
-        step(args.warmup + args.steps + k)
+        bstep(args.warmup + args.steps + k)
     torch.cuda.synchronize()
     prof = _abi.profiler_read()
     _abi.profiler_enable(False)
-    it_launch = prof.get("solve", (0, 0.0))
-    bend = prof.get("bend", (0, 0.0))
+    solve, bend = prof.get("solve", (0, 0.0)), prof.get("bend", (0, 0.0))
+    fused = prof.get("batch_fused", (0, 0.0))
     roofline = None
     peak, peak_kind = measured_peak_hbm()
-    if it_launch[0]:
-        iters = 2 * wl.substeps * wl.iterations  # per-cloth iterations in the profiled frames
-        t_iter_ms = (it_launch[1] + bend[1]) / iters  # summed over cloths
+    iters = 2 * wl.substeps * wl.iterations
+    t_iter_ms = (solve[1] + bend[1] + fused[1]) / iters if (solve[0] or fused[0]) else 0.0
+    if t_iter_ms > 0:
         ach = iteration_bytes(wl) / (t_iter_ms / 1000.0) / 1e9
         roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                    "traffic": None, "kernel": "bend+solve (one Jacobi iteration, all cloths)",
-                    "peak_source": f"{peak_kind} hbm_gbs",
-                    "stage_ms_per_frame": {k: v[1] / 2 for k, v in prof.items()}}
+                    "traffic": None, "kernel": "one Jacobi iteration over all cloths (bend + solve)",
+                    "algorithmic_bytes_per_launch": iteration_bytes(wl),
+                    "avg_iteration_ms": t_iter_ms, "peak_source": f"{peak_kind} hbm_gbs",
+                    "stage_ms_per_frame": {k: round(v[1] / 2, 4) for k, v in prof.items()}}
 
-    # ---- end to end through the C ABI with host buffers
-    n_tot = wl.num_particles
+    # ---- end to end through the C ABI: colliders from host memory every frame, all
+    # positions + normals read back into pinned host memory every frame
     host_pos = torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True)
     host_nrm = torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True)
-    offs = np.cumsum([0] + [c.num_particles for c in wl.cloths])
+    sh = vg.stream_handle(stream)
 
     def e2e_step(f):
-        plain_frame(wl, solvers, f, stream, upload_colliders=True)
-        for i, (s, spec, _) in enumerate(solvers):
-            n = spec.num_particles
-            p = host_pos.data_ptr() + 12 * int(offs[i])
-            q = host_nrm.data_ptr() + 12 * int(offs[i])
-            _abi.check(vg.lib().vt_positions_get(s.handle, 0, n, p, 1, vg.stream_handle(stream)), "positions")
-            _abi.check(vg.lib().vt_normals_get(s.handle, 0, n, q, 1, vg.stream_handle(stream)), "normals")
+        batch_frame(wl, batch, f, stream, upload_colliders=True)
+        _abi.check(vg.lib().vt_batch_all_get(batch.handle, 0, host_pos.data_ptr(), 1, sh), "all_get")
+        _abi.check(vg.lib().vt_batch_all_get(batch.handle, 1, host_nrm.data_ptr(), 1, sh), "all_get")
         stream.synchronize()
 
     for f in range(args.warmup):
         e2e_step(f)
     dist_sync()
-    t0 = time.perf_counter()
     e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
     for k in range(e2e_steps):
         e2e_step(k)
-    e2e_s = time.perf_counter() - t0
-    e2e_t = torch.tensor([e2e_s], device="cuda")
-    if dist is not None:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = pits * e2e_steps * world / float(e2e_t.item())
-    h2d = len(wl.cloths) * (2 * 208 + 128)  # colliders + domain parameter block per cloth
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = pits * e2e_steps * world / e2e_s
+    ncol = sum(len(c.colliders(0)) for c in wl.cloths)
+    h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
     d2h = n_tot * 24
+    batch.close()
+
+    # ---- the plain drop-in solver on the same workload, one cloth at a time
+    plain = None
+    if not args.no_plain:
+        solvers = build_plain_solvers(wl)
+        pstep = lambda f: plain_frame(wl, solvers, f, stream, upload_colliders=False)  # noqa: E731
+        psteps = max(3, args.steps // 4)
+        p_ms, p_per = timed_device(pstep, psteps, args.warmup, stream, dist_sync)
+        p_ms = max_over_ranks(p_ms)
+        plain = {"value": pits * psteps * world / (p_ms / 1000.0), "unit": UNIT, "steps": psteps,
+                 "ms_per_step": p_ms / psteps, "p50_frame_ms": statistics.median(p_per),
+                 "p99_frame_ms": pct(p_per, 0.99), "form": "one vt_simulate per cloth per frame, CUDA graphs"}
+        for s, _, _ in solvers:
+            s.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_single(args.workload, args.seed)
 
     if rank == 0:
-        per_sorted = sorted(per)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic grid cloths generated from the config (seeded), no dataset",
-            "config": {"workload": wl.name, "form": "plain (one cloth at a time)",
+            "config": {"workload": wl.name, "form": "batched (one graph launch per frame for all cloths)",
                        "cloths_per_gpu": len(wl.cloths), "particles_per_gpu": n_tot,
                        "substeps": wl.substeps, "iterations": wl.iterations,
                        "l2": "inputs larger than L2 (working set ~%.1f GB)" % (n_tot * 500 / 1e9),
-                       "parallelism": f"independent cloths per GPU x {world}"},
-            "p50_frame_ms": statistics.median(per), "p99_frame_ms": per_sorted[min(len(per) - 1, int(0.99 * len(per)))],
+                       "parallelism": f"independent cloths per GPU x {world} GPU(s)"},
+            "p50_frame_ms": statistics.median(per), "p99_frame_ms": pct(per, 0.99),
+            "plain": plain,
+            "batched_over_plain": (value / plain["value"]) if plain else None,
             "clocks": clock_info,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches_timed,

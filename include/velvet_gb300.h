@@ -288,8 +288,9 @@ vt_status vt_batch_normals_get(vt_batch* b, int32_t index, float* dst, int32_t d
                                void* stream);
 vt_status vt_batch_velocities_get(vt_batch* b, int32_t index, float* dst, int32_t dst_on_device,
                                   void* stream);
-/* All cloths' positions at once, cloth after cloth in index order. */
-vt_status vt_batch_all_positions_get(vt_batch* b, float* dst, int32_t dst_on_device, void* stream);
+/* Every cloth's state at once, cloth after cloth in index order: what = 0 positions,
+ * 1 normals, 2 velocities. */
+vt_status vt_batch_all_get(vt_batch* b, int32_t what, float* dst, int32_t dst_on_device, void* stream);
 
 /* Kernels enqueued by this batch so far (graph replays count their kernel nodes). */
 vt_status vt_batch_launch_count(const vt_batch* b, uint64_t* out);

@@ -236,14 +236,16 @@ vt_status vt_batch_velocities_get(vt_batch* b, int32_t index, float* dst, int32_
     return batch_get(b, index, 2, dst, on_dev, stream);
 }
 
-vt_status vt_batch_all_positions_get(vt_batch* b, float* dst, int32_t on_dev, void* stream)
+vt_status vt_batch_all_get(vt_batch* b, int32_t what, float* dst, int32_t on_dev, void* stream)
 {
     VT_CHECK(b && dst, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    VT_CHECK(what >= 0 && what <= 2, VT_ERR_INVALID_ARGUMENT, "what must be 0, 1 or 2");
     VT_CHECK(b->world.built() && !b->dirty, VT_ERR_STATE, "state exists on the device after the first simulate");
     const size_t n = (size_t)b->world.n_particles;
     if (!n) return VT_OK;
+    const float4* src = what == 0 ? b->world.d.x : what == 1 ? b->world.d.nrm : b->world.d.v;
     cudaStream_t st = (cudaStream_t)stream;
-    VT_TRY_CUDA(cudaMemcpy2DAsync(dst, 12, b->world.d.x, 16, 12, n,
+    VT_TRY_CUDA(cudaMemcpy2DAsync(dst, 12, src, 16, 12, n,
                                   on_dev ? cudaMemcpyDefault : cudaMemcpyDeviceToHost, st),
                 "copy out");
     if (!on_dev) VT_TRY_CUDA(cudaStreamSynchronize(st), "sync");

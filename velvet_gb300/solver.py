@@ -282,7 +282,7 @@ class BatchSolver:
 
     def all_positions(self) -> np.ndarray:
         out = np.empty((sum(self.sizes), 3), dtype=np.float32)
-        check(lib().vt_batch_all_positions_get(self._h, _ptr(out), 0, None), "vt_batch_all_positions_get")
+        check(lib().vt_batch_all_get(self._h, 0, _ptr(out), 0, None), "vt_batch_all_get")
         return out
 
     def launch_count(self) -> int:
