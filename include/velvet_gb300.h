@@ -329,6 +329,28 @@ vt_status vt_hash_objects(uint32_t* particle_hash, uint32_t* particle_index,
                           const float* positions, const float* original_positions,
                           const vt_hash_params* params, void* stream);
 
+/* HashObjects without any device allocation.  No counterpart in the reference: it
+ * exists for callers that cannot call cudaMalloc — an engine that hands out all device
+ * memory once at start-up and forbids allocation afterwards, a host that owns every
+ * device allocation, or a real-time frame loop where cudaMalloc / cudaFree would
+ * synchronise the device and stall the frame.  vt_hash_objects allocates its sort
+ * scratch on first use; this variant uses a fixed scratch array compiled into the
+ * library instead (about 2.2 MB, held on every GPU that loads the library until the
+ * process exits), so it accepts at most VT_HASH_NOALLOC_MAX_OBJECTS objects and returns
+ * VT_ERR_CAPACITY above that.  Same arguments, same outputs as vt_hash_objects.
+ *   - The first call on each device looks up the scratch array's device address (a
+ *     one-time set-up, no allocation); make that first call before any stream capture.
+ *   - All calls share the one array: calls whose work overlaps on the GPU (different
+ *     streams, or different host threads) race and corrupt each other's results;
+ *     serialise them on one stream.
+ *   - Nothing in the scratch needs to start at zero, so a previous call's contents do
+ *     not affect the result. */
+#define VT_HASH_NOALLOC_MAX_OBJECTS 262144
+vt_status vt_hash_objects_noalloc(uint32_t* particle_hash, uint32_t* particle_index,
+                                  uint32_t* cell_start, uint32_t* cell_end, uint32_t* neighbors,
+                                  const float* positions, const float* original_positions,
+                                  const vt_hash_params* params, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -139,6 +139,7 @@ SIGNATURES: dict[str, tuple] = {
     "vt_profiler_reset": (I32, []),
     "vt_profiler_read": (I32, [C.POINTER(VtStageTime), U32, PU32]),
     "vt_hash_objects": (I32, [P, P, P, P, P, P, P, C.POINTER(VtHashParams), P]),
+    "vt_hash_objects_noalloc": (I32, [P, P, P, P, P, P, P, C.POINTER(VtHashParams), P]),
 }
 
 _LIB: C.CDLL | None = None
