@@ -1,0 +1,184 @@
+"""GPU parity beyond the default configuration: the generic (CSR) constraint path and the
+implicit-topology grid path against each other and the oracle, and the branches of the
+reference schedule and API that the benchmark configs do not take.  Every comparison is
+bit-exact (see tests/test_gpu_parity.py)."""
+import math
+
+import numpy as np
+import pytest
+
+import velvet_gb300 as vg
+from velvet_gb300 import _abi
+from velvet_gb300 import workloads as W
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def same(a, b, what):
+    if not np.array_equal(bits(a), bits(b)):
+        d = np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64))
+        raise AssertionError(f"{what}: {(bits(a) != bits(b)).sum()} values differ, max {np.nanmax(d):.3g}")
+
+
+def spec_of(side=20, height=0.45, attached=None, colliders=None):
+    base = W.small()
+    return W.ClothSpec(side, 0.02, W.horizontal_cloth(side, 0.02, height),
+                       [0, side - 1] if attached is None else attached,
+                       colliders or base.cloths[0].colliders)
+
+
+def run_frames(solvers, spec, frames, substeps=5, iterations=10, relax=1.0, friction=0.1, margin=0.06,
+               frame_hook=None):
+    d = spec.particle_diameter()
+    for f in range(frames):
+        if frame_hook:
+            frame_hook(f)
+        for s in solvers:
+            s.update_colliders(spec.colliders(f))
+            s.simulate(float(W.FRAME_DT), substeps, iterations, relax, friction, margin, d)
+    for s in solvers:
+        if isinstance(s, vg.ClothSolver):
+            s.sync()
+
+
+def generic_copy(spec, o: Oracle, params=None):
+    """A GPU solver registered through AddStretch / AddAttachSlot / AddAttach / AddBend
+    with exactly the constraints the oracle's builder made: the CSR path."""
+    g = vg.ClothSolver(params)
+    verts, idx = spec.mesh()
+    g.add_cloth(verts, idx, spec.model, spec.particle_diameter())
+    si, sf = o.constraints(0)
+    g.add_stretch(si.reshape(-1, 2), sf)
+    pos = o.positions()
+    for p in spec.attached:
+        g.add_attach_slot(pos[p])
+    ai, af = o.constraints(1)
+    if af.size:
+        g.add_attach(ai[0::2], ai[1::2], af)
+    bi, bf = o.constraints(2)
+    g.add_bend(bi.reshape(-1, 4), bf)
+    g.update_colliders(spec.colliders(0))
+    return g
+
+
+def test_csr_path_grid_path_and_oracle_agree():
+    spec = spec_of(22)
+    o = Oracle()
+    W.build_plain(spec, o)
+    csr = generic_copy(spec, o)
+    grid = vg.ClothSolver()
+    W.build_plain(spec, grid)
+    run_frames([o, csr, grid], spec, 12)
+    same(csr.positions(), o.positions(), "csr vs oracle")
+    same(grid.positions(), o.positions(), "grid vs oracle")
+    same(grid.normals(), csr.normals(), "normals grid vs csr")
+
+
+@pytest.mark.parametrize("tile_edge", [6, 7, 8, 31, 32, 33, 40])
+def test_grid_tiles_at_every_edge_case(tile_edge):
+    """Cloth sides around the 7 x 31 tile shape: partial tiles on both axes."""
+    spec = spec_of(tile_edge, 0.4)
+    o = Oracle()
+    W.build_plain(spec, o)
+    g = vg.ClothSolver()
+    W.build_plain(spec, g)
+    run_frames([o, g], spec, 4)
+    same(g.positions(), o.positions(), f"side {tile_edge}")
+    same(g.velocities(), o.velocities(), f"side {tile_edge} velocities")
+
+
+@pytest.mark.parametrize("case", ["no_self_collision", "zero_iterations", "hash_every_substep",
+                                  "bend_compliance", "no_friction", "relaxation", "max_neighbors_8"])
+def test_schedule_branches(case):
+    p = vg.default_params()
+    kw = {}
+    if case == "no_self_collision":
+        p.enable_self_collision = 0
+    elif case == "zero_iterations":
+        kw["iterations"] = 0
+    elif case == "hash_every_substep":
+        p.interleaved_hash = 1
+    elif case == "bend_compliance":
+        p.bend_compliance = 0.5
+    elif case == "no_friction":
+        kw["friction"] = 0.0
+    elif case == "relaxation":
+        kw["relax"] = 1.4
+    elif case == "max_neighbors_8":
+        p.max_num_neighbors = 8
+    spec = spec_of(18, 0.35)
+    o, g = Oracle(p), vg.ClothSolver(p)
+    for s in (o, g):
+        W.build_plain(spec, s)
+    run_frames([o, g], spec, 6, **kw)
+    same(g.positions(), o.positions(), case)
+    same(g.velocities(), o.velocities(), case + " velocities")
+
+
+def test_two_cloths_in_one_solver_collide_like_the_reference():
+    """Several cloths in one plain solver share one hash and collide with each other
+    (VtClothSolverGPU::AddCloth merges them); the second cloth uses the CSR path."""
+    a = spec_of(16, 0.5)
+    b = spec_of(16, 0.53)
+    o, g = Oracle(), vg.ClothSolver()
+    for s in (o, g):
+        W.build_plain(a, s)
+        verts, idx = b.mesh()
+        off = s.add_cloth(verts, idx, b.model, b.particle_diameter())
+        s.build_grid_constraints(off, b.resolution, b.attached)
+        s.update_colliders(a.colliders(0))
+    run_frames([o, g], a, 8)
+    same(g.positions(), o.positions(), "merged cloths")
+    hv = o.hash_view()
+    assert np.array_equal(g.debug_view(_abi.DEBUG_PARTICLE_INDEX), hv["particle_index"])
+
+
+def test_cube_collider_and_moving_slot_and_grabber_edits():
+    cube = W.make_collider(_abi.COLLIDER_CUBE, W.model_matrix((0.05, 0.2, 0.0), (0, 30, 10), (0.5, 0.4, 0.6)),
+                           W.model_matrix((0.0, 0.2, 0.0), (0, 25, 10), (0.5, 0.4, 0.6)),
+                           (0.05, 0.2, 0.0), (0.5, 0.4, 0.6))
+    spec = spec_of(20, 0.5, colliders=W.static_colliders([cube, W.plane(0.0)]))
+    o, g = Oracle(), vg.ClothSolver()
+    for s in (o, g):
+        W.build_plain(spec, s)
+    n = spec.num_particles
+
+    def hook(f):
+        if f == 2:  # MouseGrabber: pin a particle and drag it (Velvet/MouseGrabber.hpp:45-76)
+            for s in (o, g):
+                w = np.zeros(1, np.float32)
+                s.set_inv_mass(w, first=n // 2)
+                xyz = s.positions()[n // 2] + np.float32(0.01)
+                s.set_positions(xyz.reshape(1, 3), first=n // 2)
+        if f >= 3:  # swirl scene: move attach slot 0 (Velvet/main.cpp:326-331)
+            t = f * float(W.FRAME_DT) * 3
+            pos = np.array([math.sin(t) * 0.1, 0.6, 0.2], np.float32)
+            for s in (o, g):
+                s.set_attach_slot(0, pos)
+
+    run_frames([o, g], spec, 7, frame_hook=hook)
+    same(g.positions(), o.positions(), "cube + grabber + slot")
+    same(g.inv_mass(), o.inv_mass(), "inverse masses")
+
+
+def test_state_round_trip_and_numeric_fault_flag():
+    spec = spec_of(12, 0.4)
+    g = vg.ClothSolver()
+    W.build_plain(spec, g)
+    run_frames([g], spec, 2)
+    x = g.positions()
+    g.set_positions(x)
+    same(g.positions(), x, "positions round trip")
+    v = g.velocities()
+    v[5] = np.nan  # a NaN injected on the host must be reported, not crash
+    g.set_velocities(v)
+    g.simulate(float(W.FRAME_DT), 2, 2, 1.0, 0.1, 0.06, spec.particle_diameter())
+    with pytest.raises(vg.VtError) as e:
+        g.sync()
+    assert e.value.status == _abi.VT_ERR_NUMERIC
+    g.sync()  # the flag is cleared once reported

@@ -180,6 +180,7 @@ vt_status vt_cloth_add(vt_solver* s, const float* xyz, uint32_t nv, const uint32
     vt_status st = make_topology_change(s);
     if (st != VT_OK) return st;
     HostSolver& h = s->h;
+    h.grid_res = -1;
     const int32_t prev = (int32_t)h.n();
     ClothRec c{prev, (int32_t)nv, (int32_t)(h.tri.size() / 3), (int32_t)(nidx / 3)};
     h.cloths.push_back(c);
@@ -213,6 +214,7 @@ vt_status vt_stretch_add(vt_solver* s, const int32_t* pairs, const float* rest, 
     VT_GUARD_BEGIN
     vt_status st = make_topology_change(s);
     if (st != VT_OK) return st;
+    s->h.grid_res = -1;
     s->h.st_idx.insert(s->h.st_idx.end(), pairs, pairs + 2 * (size_t)count);
     s->h.st_rest.insert(s->h.st_rest.end(), rest, rest + count);
     return VT_OK;
@@ -247,6 +249,7 @@ vt_status vt_attach_add(vt_solver* s, const int32_t* particles, const int32_t* s
     VT_GUARD_BEGIN
     vt_status st = make_topology_change(s);
     if (st != VT_OK) return st;
+    s->h.grid_res = -1;
     for (uint32_t c = 0; c < count; ++c) {
         if (distances[c] == 0) s->h.w[particles[c]] = 0;  // VtClothSolverGPU.hpp:172
         AttachOp a{};
@@ -274,6 +277,7 @@ vt_status vt_attach_generate_lra(vt_solver* s, int32_t first_slot, uint32_t num_
     vt_status st = make_topology_change(s);
     if (st != VT_OK) return st;
     HostSolver& h = s->h;
+    h.grid_res = -1;
     // The device recomputes |slot0 - x0_i|; that equals the distance the reference
     // stores only while the particles still sit at their initial positions.
     bool at_rest = true;
@@ -324,6 +328,7 @@ vt_status vt_bend_add(vt_solver* s, const uint32_t* quads, const float* rest_ang
     VT_GUARD_BEGIN
     vt_status st = make_topology_change(s);
     if (st != VT_OK) return st;
+    s->h.grid_res = -1;
     s->h.bd_idx.insert(s->h.bd_idx.end(), quads, quads + 4 * (size_t)count);
     s->h.bd_rest.insert(s->h.bd_rest.end(), rest_angles, rest_angles + count);
     return VT_OK;
@@ -350,6 +355,12 @@ vt_status vt_cloth_build_grid_constraints(vt_solver* s, int32_t offset, int32_t 
     vt_status st = make_topology_change(s);
     if (st != VT_OK) return st;
     HostSolver& h = s->h;
+    // The implicit-topology kernel applies when this is the solver's only cloth, nothing
+    // else is registered, and the positions are still the initial ones (its rest lengths
+    // are recomputed from the initial positions).
+    const bool grid_candidate = h.cloths.size() == 1 && cl.offset == 0 && h.st_rest.empty() &&
+                                h.at_ops.empty() && h.bd_rest.empty() && h.x == h.x0;
+    const int32_t first_slot = (int32_t)h.nslots();
     auto P = [&](int i) { const size_t q = 3 * (size_t)(cl.offset + i); return mk3(h.x[q], h.x[q + 1], h.x[q + 2]); };
     auto VAT = [res](int a, int b) { return a * (res + 1) + b; };
     auto add = [&](int i1, int i2) {
@@ -387,6 +398,31 @@ vt_status vt_cloth_build_grid_constraints(vt_solver* s, int32_t offset, int32_t 
         h.bd_idx.push_back(ind[i + 2]);
         h.bd_idx.push_back(ind[i + 1]);
         h.bd_rest.push_back(0.0f);
+    }
+    h.grid_res = -1;
+    if (grid_candidate) {
+        // bending must be one constraint per quad (x, y), in x-major order, over
+        // ((x,y), (x+1,y+1), (x,y+1), (x+1,y)): true for GenerateClothMesh's triangles
+        bool ok = (int64_t)h.nbend() == (int64_t)res * res;
+        for (int32_t xq = 0; ok && xq < res; ++xq)
+            for (int32_t yq = 0; ok && yq < res; ++yq) {
+                const uint32_t* q = &h.bd_idx[4 * ((size_t)xq * res + yq)];
+                ok = q[0] == (uint32_t)VAT(xq, yq) && q[1] == (uint32_t)VAT(xq + 1, yq + 1) &&
+                     q[2] == (uint32_t)VAT(xq, yq + 1) && q[3] == (uint32_t)VAT(xq + 1, yq);
+            }
+        // attachments: nothing, or one LRA group of the whole cloth over the new slots
+        if (ok && nat) {
+            ok = h.at_ops.size() == 1 && h.at_ops[0].kind == 1 && h.at_ops[0].slot_begin == first_slot &&
+                 h.at_ops[0].slot_count == (int32_t)nat && h.at_ops[0].p_begin == 0 &&
+                 h.at_ops[0].p_count == cl.count;
+        } else if (ok) {
+            ok = h.at_ops.empty();
+        }
+        if (ok) {
+            h.grid_res = res;
+            h.grid_slot_begin = first_slot;
+            h.grid_slot_count = (int32_t)nat;
+        }
     }
     return VT_OK;
     VT_GUARD_END

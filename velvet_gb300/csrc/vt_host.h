@@ -45,6 +45,13 @@ struct HostSolver {
     std::vector<vt_sdf_collider> colliders;
     float cell_spacing = 0.0f;
     int32_t table_size = 0;
+    // Set when the solver holds exactly one grid cloth whose constraints are exactly what
+    // vt_cloth_build_grid_constraints generates (verified element by element), so the
+    // implicit-topology kernel computes the same sums as the CSR kernels: the grid
+    // resolution, and the LRA slot range (local slot indices).
+    int32_t grid_res = -1;
+    int32_t grid_slot_begin = 0, grid_slot_count = 0;
+    bool use_grid_kernel = true;
 
     uint32_t n() const { return (uint32_t)(x.size() / 3); }
     uint32_t nbend() const { return (uint32_t)bd_rest.size(); }
@@ -56,7 +63,7 @@ struct HostSolver {
 // Per-stage GPU timing (vt_profiler_*): event pairs around stage launches.
 enum Stage {
     ST_PRESDF_PREDICT, ST_HASH_KEYS, ST_RADIX_SORT, ST_CELL_RANGES, ST_CACHE_NEIGHBORS,
-    ST_COLLIDE, ST_BEND, ST_SOLVE, ST_FINALIZE, ST_NORMALS, ST_BATCH_FUSED, ST_COUNT
+    ST_COLLIDE, ST_BEND, ST_SOLVE, ST_FINALIZE, ST_NORMALS, ST_GRID_ITER, ST_COUNT
 };
 const char* stage_name(int stage);
 bool profiler_on();
@@ -119,6 +126,7 @@ public:
     std::vector<float4> hslots;
     int32_t n_domains = 0, n_particles = 0, n_bends = 0, n_slots = 0, n_cols = 0;
     int32_t total_keys = 0, n_ptiles = 0, n_btiles = 0, nbr_words = 0;
+    int32_t n_stiles = 0, n_gtiles = 0;
     int32_t pcur = 0;  // which of p[0], p[1] holds the latest predicted positions
     uint64_t bytes = 0;
     uint64_t launches = 0;  // kernels enqueued so far

@@ -196,9 +196,118 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
     pout[i] = make_float4(pi.x, pi.y, pi.z, wi);
 }
 
-// ------------------------------------------------------------------ bending
-// SolveBending_Kernel (VtClothSolverGPU.cu:117-189), once per constraint; the four
-// corrections go to per-corner slots (w = 1 when the constraint fired).
+// ------------------------------------------------------------------ constraint math
+// One dihedral bending constraint, SolveBending_Kernel (VtClothSolverGPU.cu:117-189).
+// a0..a3: predicted positions with the inverse mass in w.  Writes the four corrections
+// with w = 1 when the constraint fired, all zero when it returned early.
+__device__ __forceinline__ void bend_eval(float4 a0, float4 a1, float4 a2, float4 a3, float rest,
+                                          float bend_compliance, float dt, float4& c0, float4& c1,
+                                          float4& c2, float4& c3)
+{
+    const vec3 p0 = xyz(a0), p1 = xyz(a1), p2 = xyz(a2), p3 = xyz(a3);
+    const float w0 = a0.w, w1 = a1.w, w2 = a2.w, w3 = a3.w;
+    c0 = make_float4(0, 0, 0, 0);
+    c1 = c0;
+    c2 = c0;
+    c3 = c0;
+    const vec3 e = p3 - p2;
+    const float elen = length(e);
+    if (elen < VT_EPSILON) return;
+    const float inv = 1.0f / elen;
+    vec3 n1 = cross(p2 - p0, p3 - p0);
+    n1 = n1 / dot(n1, n1);
+    vec3 n2 = cross(p3 - p1, p2 - p1);
+    n2 = n2 / dot(n2, n2);
+    const vec3 d0 = n1 * elen;
+    const vec3 d1 = n2 * elen;
+    const vec3 d2 = n1 * (dot(p0 - p3, e) * inv) + n2 * (dot(p1 - p3, e) * inv);
+    const vec3 d3 = n1 * (dot(p2 - p0, e) * inv) + n2 * (dot(p2 - p1, e) * inv);
+    n1 = normalize(n1);
+    n2 = normalize(n2);
+    const float phi = vt_acosf(gclamp(dot(n1, n2), -1.0f, 1.0f));
+    float lambda = w0 * dot(d0, d0) + w1 * dot(d1, d1);
+    lambda = lambda + w2 * dot(d2, d2);
+    lambda = lambda + w3 * dot(d3, d3);
+    if (lambda < VT_EPSILON) return;
+    const float xpbd = bend_compliance / dt / dt;
+    lambda = (phi - rest) / (lambda + xpbd);
+    if (dot(cross(n1, n2), e) > 0.0f) lambda = -lambda;
+    const vec3 k0 = d0 * (-w0 * lambda), k1 = d1 * (-w1 * lambda);
+    const vec3 k2 = d2 * (-w2 * lambda), k3 = d3 * (-w3 * lambda);
+    c0 = make_float4(k0.x, k0.y, k0.z, 1.0f);
+    c1 = make_float4(k1.x, k1.y, k1.z, 1.0f);
+    c2 = make_float4(k2.x, k2.y, k2.z, 1.0f);
+    c3 = make_float4(k3.x, k3.y, k3.z, 1.0f);
+}
+
+// One distance constraint, SolveStretch_Kernel (VtClothSolverGPU.cu:76-98): returns
+// whether it fires and `common` = lambda * gradient, gradient taken from pa - pb.  The
+// reference adds -w_a * common to a and w_b * common to b.  Evaluated from the other
+// endpoint (pa, pb swapped) every intermediate value is the exact negation, so either
+// endpoint may evaluate it.
+__device__ __forceinline__ bool stretch_common(float4 pa, float4 pb, float rest, vec3& common)
+{
+    const vec3 diff = xyz(pa) - xyz(pb);
+    const float d = length(diff);
+    const float denom = pa.w + pb.w;
+    if (!(d != rest && denom > 0)) return false;
+    const vec3 grad = diff / (d + VT_EPSILON);
+    const float lambda = (d - rest) / denom;
+    common = grad * lambda;
+    return true;
+}
+
+// One attachment, SolveAttachment_Kernel (VtClothSolverGPU.cu:216-234).
+__device__ __forceinline__ void attach_one(vec3 pi, float wi, vec3 slot, float target, vec3& acc, int& cnt)
+{
+    if (wi == 0 && target > 0) return;
+    const vec3 diff = pi - slot;
+    const float d = length(diff);
+    if (d > target) {
+        acc3(acc, (-diff) + (diff / d) * target);
+        cnt++;
+    }
+}
+
+// ApplyDeltas (VtClothSolverGPU.cu:253-264) and, by mode, Finalize (:388-407) and the
+// next substep's PredictPositions (:42-53); writes x, v, p_out of particle i.
+template <int kMode>
+__device__ __forceinline__ void apply_and_finalize(const DomainParams& D, int dom, int i, vec3 pi, float wi,
+                                                   vec3 acc, int cnt, float4* __restrict__ pout,
+                                                   float4* __restrict__ x, float4* __restrict__ v,
+                                                   int32_t* __restrict__ status)
+{
+    if (cnt > 0) {
+        const float count = (float)cnt;
+        pi = pi + (acc / count) * D.relax;
+    }
+    if (kMode == SOLVE_PLAIN) {
+        pout[i] = make_float4(pi.x, pi.y, pi.z, wi);
+        return;
+    }
+    const float dt = D.dt_sub;
+    const float4 x4 = x[i];
+    const vec3 xi = xyz(x4);
+    vec3 np = pi;
+    vec3 rv = (np - xi) / dt;
+    const float rl = length(rv);
+    if (rl > D.max_speed) {
+        rv = (rv / rl) * D.max_speed;
+        np = xi + rv * dt;
+    }
+    vec3 vn = rv * (1.0f - D.damping * dt);
+    flag_nonfinite(status, D, dom, np);
+    x[i] = make_float4(np.x, np.y, np.z, x4.w);
+    if (kMode == SOLVE_FINALIZE_PREDICT) {
+        vn = vn + mk3(D.gx, D.gy, D.gz) * dt;
+        pi = np + vn * dt;
+    }
+    v[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
+    pout[i] = make_float4(pi.x, pi.y, pi.z, x4.w);
+}
+
+// ------------------------------------------------------------------ bending (CSR domains)
+// SolveBending once per constraint; the four corrections go to per-corner slots.
 __global__ void __launch_bounds__(kBlock)
 k_bend(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
        const float4* __restrict__ pin, const uint4* __restrict__ bidx,
@@ -209,42 +318,8 @@ k_bend(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
     if (b >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
     const uint4 q = bidx[b];
-    const float rest = brest[b];
-    const float4 a0 = pin[q.x], a1 = pin[q.y], a2 = pin[q.z], a3 = pin[q.w];
-    const vec3 p0 = xyz(a0), p1 = xyz(a1), p2 = xyz(a2), p3 = xyz(a3);
-    const float w0 = a0.w, w1 = a1.w, w2 = a2.w, w3 = a3.w;
-    float4 c0 = make_float4(0, 0, 0, 0), c1 = c0, c2 = c0, c3 = c0;
-    const vec3 e = p3 - p2;
-    const float elen = length(e);
-    if (!(elen < VT_EPSILON)) {
-        const float inv = 1.0f / elen;
-        vec3 n1 = cross(p2 - p0, p3 - p0);
-        n1 = n1 / dot(n1, n1);
-        vec3 n2 = cross(p3 - p1, p2 - p1);
-        n2 = n2 / dot(n2, n2);
-        const vec3 d0 = n1 * elen;
-        const vec3 d1 = n2 * elen;
-        const vec3 d2 = n1 * (dot(p0 - p3, e) * inv) + n2 * (dot(p1 - p3, e) * inv);
-        const vec3 d3 = n1 * (dot(p2 - p0, e) * inv) + n2 * (dot(p2 - p1, e) * inv);
-        n1 = normalize(n1);
-        n2 = normalize(n2);
-        const float phi = vt_acosf(gclamp(dot(n1, n2), -1.0f, 1.0f));
-        float lambda = w0 * dot(d0, d0) + w1 * dot(d1, d1);
-        lambda = lambda + w2 * dot(d2, d2);
-        lambda = lambda + w3 * dot(d3, d3);
-        if (!(lambda < VT_EPSILON)) {
-            const float dt = D.dt_sub;
-            const float xpbd = D.bend_compliance / dt / dt;
-            lambda = (phi - rest) / (lambda + xpbd);
-            if (dot(cross(n1, n2), e) > 0.0f) lambda = -lambda;
-            vec3 k0 = d0 * (-w0 * lambda), k1 = d1 * (-w1 * lambda);
-            vec3 k2 = d2 * (-w2 * lambda), k3 = d3 * (-w3 * lambda);
-            c0 = make_float4(k0.x, k0.y, k0.z, 1.0f);
-            c1 = make_float4(k1.x, k1.y, k1.z, 1.0f);
-            c2 = make_float4(k2.x, k2.y, k2.z, 1.0f);
-            c3 = make_float4(k3.x, k3.y, k3.z, 1.0f);
-        }
-    }
+    float4 c0, c1, c2, c3;
+    bend_eval(pin[q.x], pin[q.y], pin[q.z], pin[q.w], brest[b], D.bend_compliance, D.dt_sub, c0, c1, c2, c3);
     float4* out = bcorr + 4 * (size_t)b;
     out[0] = c0;
     out[1] = c1;
@@ -252,11 +327,10 @@ k_bend(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
     out[3] = c3;
 }
 
-// ------------------------------------------------------------------ constraint gather
+// ------------------------------------------------------------------ constraint gather (CSR)
 // SolveStretch (:65-102) + SolveAttachment (:205-235) + the bending corners written by
-// k_bend, summed per particle in constraint order, then ApplyDeltas (:253-264).  With
-// `fin` set, Finalize (:388-407) follows, and with SOLVE_FINALIZE_PREDICT the next
-// substep's PredictPositions (:42-53).
+// k_bend, summed per particle in constraint order, then ApplyDeltas (:253-264) and, by
+// mode, Finalize + the next Predict.  For domains whose topology is arbitrary.
 template <int kMode>
 __global__ void __launch_bounds__(kBlock)
 k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
@@ -274,104 +348,191 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
     if (i >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
     const float4 pi4 = pin[i];
-    vec3 pi = xyz(pi4);
+    const vec3 pi = xyz(pi4);
     const float wi = pi4.w;
     vec3 acc = mk3(0, 0, 0);
     int cnt = 0;
-
-    // stretch: each entry is (other particle, rest length)
-    {
-        const int e0 = st_off[i], e1 = st_off[i + 1];
-        for (int e = e0; e < e1; ++e) {
-            const int2 en = st_ent[e];
-            const float4 pj4 = pin[en.x];
-            const float rest = __int_as_float(en.y);
-            const vec3 diff = pi - xyz(pj4);
-            const float d = length(diff);
-            const float denom = wi + pj4.w;
-            if (d != rest && denom > 0) {
-                const vec3 grad = diff / (d + VT_EPSILON);
-                const float lambda = (d - rest) / denom;
-                const vec3 common = grad * lambda;
-                acc3(acc, common * (-wi));
-                cnt++;
-            }
+    // stretch: each entry is (other particle, rest length); this particle evaluates the
+    // constraint as its first endpoint and takes -w_i * common
+    for (int e = st_off[i], e1 = st_off[i + 1]; e < e1; ++e) {
+        const int2 en = st_ent[e];
+        vec3 common;
+        if (stretch_common(pi4, pin[en.x], __int_as_float(en.y), common)) {
+            acc3(acc, common * (-wi));
+            cnt++;
         }
     }
     // attachments: (slot, distance) or an LRA group (distances recomputed from x0)
-    {
-        const int e0 = at_off[i], e1 = at_off[i + 1];
-        const float lrs = D.lrs;
-        for (int e = e0; e < e1; ++e) {
-            const int2 en = at_ent[e];
-            if (en.x >= 0) {
-                const float target = __int_as_float(en.y) * lrs;
-                if (wi == 0 && target > 0) continue;
-                const vec3 diff = pi - xyz(slots[en.x]);
-                const float d = length(diff);
-                if (d > target) {
-                    acc3(acc, (-diff) + (diff / d) * target);
-                    cnt++;
-                }
-            } else {
-                const LraGroup g = lra[-en.x - 1];
-                const vec3 x0i = xyz(x0[i]);
-                for (int s = g.slot_begin; s < g.slot_begin + g.slot_count; ++s) {
-                    const float rest = length(xyz(slots0[s]) - x0i);
-                    const float target = rest * lrs;
-                    if (wi == 0 && target > 0) continue;
-                    const vec3 diff = pi - xyz(slots[s]);
-                    const float d = length(diff);
-                    if (d > target) {
-                        acc3(acc, (-diff) + (diff / d) * target);
-                        cnt++;
-                    }
-                }
+    const float lrs = D.lrs;
+    for (int e = at_off[i], e1 = at_off[i + 1]; e < e1; ++e) {
+        const int2 en = at_ent[e];
+        if (en.x >= 0) {
+            attach_one(pi, wi, xyz(slots[en.x]), __int_as_float(en.y) * lrs, acc, cnt);
+        } else {
+            const LraGroup g = lra[-en.x - 1];
+            const vec3 x0i = xyz(x0[i]);
+            for (int s = g.slot_begin; s < g.slot_begin + g.slot_count; ++s) {
+                const float rest = length(xyz(slots0[s]) - x0i);
+                attach_one(pi, wi, xyz(slots[s]), rest * lrs, acc, cnt);
             }
         }
     }
     // bending corners
-    {
-        const int e0 = bd_off[i], e1 = bd_off[i + 1];
-        for (int e = e0; e < e1; ++e) {
-            const float4 c = bcorr[bd_ent[e]];
-            if (c.w != 0.0f) {
-                acc3(acc, xyz(c));
-                cnt++;
-            }
+    for (int e = bd_off[i], e1 = bd_off[i + 1]; e < e1; ++e) {
+        const float4 c = bcorr[bd_ent[e]];
+        if (c.w != 0.0f) {
+            acc3(acc, xyz(c));
+            cnt++;
         }
     }
-    if (cnt > 0) {
-        const float count = (float)cnt;
-        pi = pi + (acc / count) * D.relax;
-    }
-    if (kMode == SOLVE_PLAIN) {
-        pout[i] = make_float4(pi.x, pi.y, pi.z, wi);
-        return;
-    }
-    // Finalize
-    const float dt = D.dt_sub;
-    const float4 x4 = x[i];
-    const vec3 xi = xyz(x4);
-    vec3 np = pi;
-    vec3 rv = (np - xi) / dt;
-    const float rl = length(rv);
-    if (rl > D.max_speed) {
-        rv = (rv / rl) * D.max_speed;
-        np = xi + rv * dt;
-    }
-    vec3 vn = rv * (1.0f - D.damping * dt);
-    flag_nonfinite(status, D, tl.dom, np);
-    x[i] = make_float4(np.x, np.y, np.z, x4.w);
-    if (kMode == SOLVE_FINALIZE_PREDICT) {
-        vn = vn + mk3(D.gx, D.gy, D.gz) * dt;
-        pi = np + vn * dt;
-    }
-    v[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
-    pout[i] = make_float4(pi.x, pi.y, pi.z, x4.w);
+    apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, pout, x, v, status);
 }
 
-// Finalize without a preceding constraint gather (zero iterations).
+// ------------------------------------------------------------------ grid tile iteration
+// One Jacobi iteration of a grid cloth built by the grid constraint builder, with its
+// topology implicit: particle (a, b) = a * V + b, stretch constraints of generator (x, y)
+// t0 (x,y)-(x,y+1), t1 (x,y)-(x+1,y), t2 (x,y)-(x+1,y+1), t3 (x,y+1)-(x+1,y) in
+// constraint order x-major / y / type (VtClothObjectGPU.hpp:75-116), bending of quad
+// (x, y) over ((x,y), (x+1,y+1), (x,y+1), (x+1,y)) (:118-132), rest lengths
+// |x0_i - x0_j| (the builder's values: registration verifies x == x0 at build time)
+// and rest angles 0.  A block owns a 7 x 31 tile; it stages the tile and a one-particle
+// halo of predicted and initial positions in shared memory, evaluates each of the
+// 8 x 32 generators touching the tile once (one per thread: one bend + four stretch
+// constraints), then each particle sums its eight stretch, the LRA and its four bending
+// corrections in constraint order — the order of the CSR kernel and of the oracle.
+constexpr int kGHA = kGridTA + 2, kGHB = kGridTB + 2;  // halo tile 9 x 33
+constexpr int kGGA = kGridTA + 1, kGGB = kGridTB + 1;  // generators 8 x 32
+
+template <int kMode>
+__global__ void __launch_bounds__(kBlock)
+k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+            const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ x,
+            float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ slots,
+            const float4* __restrict__ slots0, int32_t* __restrict__ status)
+{
+    __shared__ float4 sp[kGHA][kGHB];
+    __shared__ float4 sx0[kGHA][kGHB];
+    __shared__ float4 sst[4][kGGA][kGGB];  // stretch common + fired flag, per type
+    __shared__ float4 sbd[4][kGGA][kGGB];  // bending corner corrections + fired flag
+    const GridTile tl = tiles[blockIdx.x];
+    const DomainParams& D = doms[tl.dom];
+    const int R = D.grid_res, V = R + 1, base = D.p_begin;
+    const int a0 = tl.a0, b0 = tl.b0;
+    const int tid = (int)threadIdx.x;
+
+    // 1. halo tile of predicted and initial positions
+    for (int k = tid; k < kGHA * kGHB; k += kBlock) {
+        const int ha = k / kGHB, hb = k - ha * kGHB;
+        const int a = a0 - 1 + ha, b = b0 - 1 + hb;
+        float4 q = make_float4(0, 0, 0, 0), o = q;
+        if (a >= 0 && a < V && b >= 0 && b < V) {
+            const int i = base + a * V + b;
+            q = pin[i];
+            o = x0[i];
+        }
+        sp[ha][hb] = q;
+        sx0[ha][hb] = o;
+    }
+    __syncthreads();
+
+    // 2. generators (x, y) = (a0 - 1 + gx, b0 - 1 + gy): one per thread
+    {
+        const int gx = tid / kGGB, gy = tid - gx * kGGB;
+        const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
+        const float4 zero = make_float4(0, 0, 0, 0);
+        float4 s0 = zero, s1 = zero, s2 = zero, s3 = zero;
+        float4 c0 = zero, c1 = zero, c2 = zero, c3 = zero;
+        if (X >= 0 && Y >= 0 && X <= R && Y <= R) {
+            const float4 pxy = sp[gx][gy];
+            const vec3 oxy = xyz(sx0[gx][gy]);
+            vec3 cm;
+            if (Y < R) {  // t0: (x,y)-(x,y+1)
+                if (stretch_common(pxy, sp[gx][gy + 1], length(oxy - xyz(sx0[gx][gy + 1])), cm))
+                    s0 = make_float4(cm.x, cm.y, cm.z, 1.0f);
+            }
+            if (X < R) {  // t1: (x,y)-(x+1,y)
+                if (stretch_common(pxy, sp[gx + 1][gy], length(oxy - xyz(sx0[gx + 1][gy])), cm))
+                    s1 = make_float4(cm.x, cm.y, cm.z, 1.0f);
+            }
+            if (X < R && Y < R) {
+                // t2: (x,y)-(x+1,y+1)
+                if (stretch_common(pxy, sp[gx + 1][gy + 1], length(oxy - xyz(sx0[gx + 1][gy + 1])), cm))
+                    s2 = make_float4(cm.x, cm.y, cm.z, 1.0f);
+                // t3: (x,y+1)-(x+1,y)
+                if (stretch_common(sp[gx][gy + 1], sp[gx + 1][gy],
+                                   length(xyz(sx0[gx][gy + 1]) - xyz(sx0[gx + 1][gy])), cm))
+                    s3 = make_float4(cm.x, cm.y, cm.z, 1.0f);
+                // bend of quad (x, y): corners (x,y), (x+1,y+1), (x,y+1), (x+1,y)
+                bend_eval(pxy, sp[gx + 1][gy + 1], sp[gx][gy + 1], sp[gx + 1][gy], 0.0f,
+                          D.bend_compliance, D.dt_sub, c0, c1, c2, c3);
+            }
+        }
+        sst[0][gx][gy] = s0;
+        sst[1][gx][gy] = s1;
+        sst[2][gx][gy] = s2;
+        sst[3][gx][gy] = s3;
+        sbd[0][gx][gy] = c0;
+        sbd[1][gx][gy] = c1;
+        sbd[2][gx][gy] = c2;
+        sbd[3][gx][gy] = c3;
+    }
+    __syncthreads();
+
+    // 3. particles of the tile
+    if (tid >= kGridTA * kGridTB) return;
+    const int ta = tid / kGridTB, tb = tid - ta * kGridTB;
+    const int a = a0 + ta, b = b0 + tb;
+    if (a >= V || b >= V) return;
+    const int i = base + a * V + b;
+    const int gx = ta + 1, gy = tb + 1;  // this particle's generator (a, b) and halo slot
+    const float4 pi4 = sp[gx][gy];
+    const vec3 pi = xyz(pi4);
+    const float wi = pi4.w, nw = -wi;
+    vec3 acc = mk3(0, 0, 0);
+    int cnt = 0;
+#define VT_TAKE(s4, scale)                          \
+    do {                                            \
+        const float4 s_ = (s4);                     \
+        if (s_.w != 0.0f) {                         \
+            acc3(acc, mk3(s_.x, s_.y, s_.z) * (scale)); \
+            cnt++;                                  \
+        }                                           \
+    } while (0)
+    // stretch, constraint order: generators (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
+    if (a >= 1 && b >= 1) VT_TAKE(sst[2][gx - 1][gy - 1], wi);  // t2, second endpoint
+    if (a >= 1) VT_TAKE(sst[1][gx - 1][gy], wi);                // t1, second endpoint
+    if (a >= 1 && b < R) VT_TAKE(sst[3][gx - 1][gy], wi);       // t3, second endpoint
+    if (b >= 1) VT_TAKE(sst[0][gx][gy - 1], wi);                // t0, second endpoint
+    if (b >= 1 && a < R) VT_TAKE(sst[3][gx][gy - 1], nw);       // t3, first endpoint
+    if (b < R) VT_TAKE(sst[0][gx][gy], nw);                     // t0, first endpoint
+    if (a < R) VT_TAKE(sst[1][gx][gy], nw);                     // t1, first endpoint
+    if (a < R && b < R) VT_TAKE(sst[2][gx][gy], nw);            // t2, first endpoint
+#undef VT_TAKE
+    // long-range attachments, slot order
+    if (D.grid_slot_count) {
+        const vec3 x0i = xyz(sx0[gx][gy]);
+        for (int s = D.grid_slot_begin; s < D.grid_slot_begin + D.grid_slot_count; ++s) {
+            const float rest = length(xyz(slots0[s]) - x0i);
+            attach_one(pi, wi, xyz(slots[s]), rest * D.lrs, acc, cnt);
+        }
+    }
+    // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
+#define VT_CORNER(c4)                     \
+    do {                                  \
+        const float4 c_ = (c4);           \
+        if (c_.w != 0.0f) {               \
+            acc3(acc, xyz(c_));           \
+            cnt++;                        \
+        }                                 \
+    } while (0)
+    if (a >= 1 && b >= 1) VT_CORNER(sbd[1][gx - 1][gy - 1]);
+    if (a >= 1 && b < R) VT_CORNER(sbd[3][gx - 1][gy]);
+    if (a < R && b >= 1) VT_CORNER(sbd[2][gx][gy - 1]);
+    if (a < R && b < R) VT_CORNER(sbd[0][gx][gy]);
+#undef VT_CORNER
+    apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, pout, x, v, status);
+}
+
 template <int kPredict>
 __global__ void __launch_bounds__(kBlock)
 k_finalize(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
@@ -453,18 +614,33 @@ cudaError_t launch_bend(const Launch& L, int pin)
 
 cudaError_t launch_solve(const Launch& L, int pin, int pout, int mode)
 {
-    if (!L.n_ptiles) return cudaSuccess;
+    if (!L.n_stiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
 #define VT_SOLVE_ARGS                                                                      \
-    d.ptiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.st_off, d.st_ent, d.at_off,    \
+    d.stiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.st_off, d.st_ent, d.at_off,    \
         d.at_ent, d.lra, d.slots, d.slots0, d.bd_off, d.bd_ent, d.bd_corr, d.status
     if (mode == SOLVE_PLAIN)
-        k_solve<SOLVE_PLAIN><<<L.n_ptiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
+        k_solve<SOLVE_PLAIN><<<L.n_stiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
     else if (mode == SOLVE_FINALIZE)
-        k_solve<SOLVE_FINALIZE><<<L.n_ptiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
+        k_solve<SOLVE_FINALIZE><<<L.n_stiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
     else
-        k_solve<SOLVE_FINALIZE_PREDICT><<<L.n_ptiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
+        k_solve<SOLVE_FINALIZE_PREDICT><<<L.n_stiles, kBlock, 0, L.st>>>(VT_SOLVE_ARGS);
 #undef VT_SOLVE_ARGS
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int mode)
+{
+    if (!L.n_gtiles) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+#define VT_GRID_ARGS d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.slots, d.slots0, d.status
+    if (mode == SOLVE_PLAIN)
+        k_grid_iter<SOLVE_PLAIN><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+    else if (mode == SOLVE_FINALIZE)
+        k_grid_iter<SOLVE_FINALIZE><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+    else
+        k_grid_iter<SOLVE_FINALIZE_PREDICT><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+#undef VT_GRID_ARGS
     return cudaGetLastError();
 }
 

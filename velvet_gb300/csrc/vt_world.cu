@@ -97,7 +97,7 @@ const char* stage_name(int s)
 {
     static const char* names[ST_COUNT] = {"presdf_predict", "hash_keys", "radix_sort", "cell_ranges",
                                           "cache_neighbors", "collide", "bend", "solve", "finalize",
-                                          "normals", "batch_fused"};
+                                          "normals", "grid_iter"};
     return (s >= 0 && s < ST_COUNT) ? names[s] : "?";
 }
 
@@ -265,10 +265,14 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
 {
     release();
     n_domains = (int32_t)S.size();
+    // domains solved by the implicit-topology grid kernel (their CSR rows stay empty)
+    std::vector<char> grid(S.size());
+    for (size_t k = 0; k < S.size(); ++k) grid[k] = S[k]->grid_res >= 1 && S[k]->use_grid_kernel;
     int64_t N = 0, B = 0, SL = 0, C = 0, G = 0, TR = 0, TK = 0, NW = 0;
-    for (const HostSolver* h : S) {
+    for (size_t k = 0; k < S.size(); ++k) {
+        const HostSolver* h = S[k];
         N += h->n();
-        B += h->nbend();
+        B += grid[k] ? 0 : h->nbend();
         SL += h->nslots();
         C += (int64_t)h->colliders.size();
         TR += (int64_t)h->tri.size() / 3;
@@ -302,15 +306,22 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     at.init(N);
     bd.init(N);
     tn.init(N);
-    std::vector<Tile> pt, bt;
+    std::vector<Tile> pt, st_tiles, bt;
+    std::vector<GridTile> gt;
     hdom.assign(n_domains, DomainParams{});
     hcol.clear();
 
     int32_t pb = 0, bb = 0, sb = 0, tb = 0, tkb = 0, nwb = 0, gb = 0, cb = 0;
     // pass 1: counts
     {
-        int32_t p0 = 0, b0 = 0, t0 = 0;
-        for (const HostSolver* h : S) {
+        int32_t p0 = 0;
+        for (size_t k = 0; k < S.size(); ++k) {
+            const HostSolver* h = S[k];
+            for (size_t q = 0; q < h->tri.size() / 3 * 3; ++q) tn.count(p0 + (int32_t)h->tri[q]);
+            if (grid[k]) {
+                p0 += (int32_t)h->n();
+                continue;
+            }
             for (size_t c = 0; c < h->st_rest.size(); ++c) {
                 st.count(p0 + h->st_idx[2 * c]);
                 st.count(p0 + h->st_idx[2 * c + 1]);
@@ -320,14 +331,9 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
                 else
                     for (int32_t i = 0; i < a.p_count; ++i) at.count(p0 + a.p_begin + i);
             }
-            for (size_t k = 0; k < h->bd_idx.size(); ++k) bd.count(p0 + (int32_t)h->bd_idx[k]);
-            for (size_t k = 0; k < h->tri.size() / 3 * 3; ++k) tn.count(p0 + (int32_t)h->tri[k]);
+            for (size_t q = 0; q < h->bd_idx.size(); ++q) bd.count(p0 + (int32_t)h->bd_idx[q]);
             p0 += (int32_t)h->n();
-            b0 += (int32_t)h->nbend();
-            t0 += (int32_t)(h->tri.size() / 3);
         }
-        (void)b0;
-        (void)t0;
     }
     st.finish_counts();
     at.finish_counts();
@@ -349,7 +355,8 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
             hslot[sb + s] = make_float4(h.slots[3 * s], h.slots[3 * s + 1], h.slots[3 * s + 2], 0.0f);
             hslot0[sb + s] = make_float4(h.slots0[3 * s], h.slots0[3 * s + 1], h.slots0[3 * s + 2], 0.0f);
         }
-        for (size_t c = 0; c < h.st_rest.size(); ++c) {
+        const bool g = grid[k] != 0;
+        for (size_t c = 0; !g && c < h.st_rest.size(); ++c) {
             const int32_t a = pb + h.st_idx[2 * c], b = pb + h.st_idx[2 * c + 1];
             int32_t rb;
             std::memcpy(&rb, &h.st_rest[c], 4);
@@ -357,6 +364,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
             st.put(b, make_int2(a, rb));
         }
         for (const AttachOp& a : h.at_ops) {
+            if (g) break;
             if (a.kind == 0) {
                 int32_t db;
                 std::memcpy(&db, &a.dist, 4);
@@ -372,7 +380,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
                 for (int32_t i = 0; i < a.p_count; ++i) at.put(pb + a.p_begin + i, make_int2(-(gid + 1), 0));
             }
         }
-        for (uint32_t c = 0; c < h.nbend(); ++c) {
+        for (uint32_t c = 0; !g && c < h.nbend(); ++c) {
             const uint32_t* q = &h.bd_idx[4 * c];
             hbd[bb + c] = make_uint4(pb + q[0], pb + q[1], pb + q[2], pb + q[3]);
             hbr[bb + c] = h.bd_rest[c];
@@ -398,10 +406,21 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         D.cell_spacing = h.cell_spacing;
         D.cell_spacing2 = h.cell_spacing * h.cell_spacing;
         tiles_for(pt, k, pb, n);
-        tiles_for(bt, k, bb, (int32_t)h.nbend());
+        if (g) {
+            D.grid_res = h.grid_res;
+            D.grid_slot_begin = sb + h.grid_slot_begin;
+            D.grid_slot_count = h.grid_slot_count;
+            const int32_t V = h.grid_res + 1;
+            for (int32_t a = 0; a < V; a += kGridTA)
+                for (int32_t b = 0; b < V; b += kGridTB) gt.push_back(GridTile{k, a, b, 0});
+        } else {
+            D.grid_res = 0;
+            tiles_for(st_tiles, k, pb, n);
+            tiles_for(bt, k, bb, (int32_t)h.nbend());
+            bb += (int32_t)h.nbend();
+        }
 
         pb += n;
-        bb += (int32_t)h.nbend();
         sb += (int32_t)h.nslots();
         tb += ntri;
         tkb += h.table_size + 1;
@@ -410,6 +429,8 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     }
     n_ptiles = (int32_t)pt.size();
     n_btiles = (int32_t)bt.size();
+    n_stiles = (int32_t)st_tiles.size();
+    n_gtiles = (int32_t)gt.size();
     hslots = hslot;
 
     // ---- device arena
@@ -429,6 +450,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_cs = A.take<uint32_t>(TK), o_ce = A.take<uint32_t>(TK), o_nb = A.take<uint32_t>(NW);
     const size_t o_dom = A.take<DomainParams>(n_domains), o_col = A.take<ColliderDev>(C);
     const size_t o_pt = A.take<Tile>(pt.size()), o_bt = A.take<Tile>(bt.size());
+    const size_t o_stt = A.take<Tile>(st_tiles.size()), o_gt = A.take<GridTile>(gt.size());
     const size_t o_st = A.take<int32_t>(1 + n_domains);
     bytes = A.off;
     VT_CUDA(cudaMalloc(&arena_, A.off), "cudaMalloc(world)");
@@ -448,6 +470,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     d.cell_start = AT(uint32_t, o_cs); d.cell_end = AT(uint32_t, o_ce); d.nbr = AT(uint32_t, o_nb);
     d.dom = AT(DomainParams, o_dom); d.col = AT(ColliderDev, o_col);
     d.ptiles = AT(Tile, o_pt); d.btiles = AT(Tile, o_bt); d.status = AT(int32_t, o_st);
+    d.stiles = AT(Tile, o_stt); d.gtiles = AT(GridTile, o_gt);
 #undef AT
     auto up = [](void* dst, const void* src, size_t bytes_) -> cudaError_t {
         return bytes_ ? cudaMemcpy(dst, src, bytes_, cudaMemcpyHostToDevice) : cudaSuccess;
@@ -477,6 +500,8 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     VT_CUDA(cudaMemset(d.nbr, 0xff, (size_t)NW * 4), "memset nbr");
     VT_CUDA(up(d.ptiles, pt.data(), pt.size() * sizeof(Tile)), "upload ptiles");
     VT_CUDA(up(d.btiles, bt.data(), bt.size() * sizeof(Tile)), "upload btiles");
+    VT_CUDA(up(d.stiles, st_tiles.data(), st_tiles.size() * sizeof(Tile)), "upload stiles");
+    VT_CUDA(up(d.gtiles, gt.data(), gt.size() * sizeof(GridTile)), "upload gtiles");
     VT_CUDA(cudaMemset(d.status, 0, (1 + n_domains) * 4), "memset status");
 
     staging_bytes_ = sizeof(DomainParams) * n_domains + sizeof(ColliderDev) * C + 16 * SL + 64;
@@ -617,7 +642,7 @@ vt_status World::upload_frame(cudaStream_t st)
 
 vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cudaStream_t st)
 {
-    Launch L{&d, n_ptiles, n_btiles, n_particles, st};
+    Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles};
     int pc = 0;
     int bits = 0;
     while ((1ll << bits) < (int64_t)total_keys) ++bits;
@@ -649,7 +674,8 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
             if (n_btiles) VT_STAGE(ST_BEND, launch_bend(L, pc), "bend", bk);
             const int mode = it < a.iterations - 1 ? SOLVE_PLAIN
                                                    : (last_sub ? SOLVE_FINALIZE : SOLVE_FINALIZE_PREDICT);
-            VT_STAGE(ST_SOLVE, launch_solve(L, pc, 1 - pc, mode), "solve", pk);
+            if (n_stiles) VT_STAGE(ST_SOLVE, launch_solve(L, pc, 1 - pc, mode), "solve", 1);
+            if (n_gtiles) VT_STAGE(ST_GRID_ITER, launch_grid_iter(L, pc, 1 - pc, mode), "grid_iter", 1);
             pc = 1 - pc;
         }
         if (a.iterations == 0)

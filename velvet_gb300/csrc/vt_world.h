@@ -42,8 +42,17 @@ struct DomainParams {
     float dt_frame, dt_sub;
     float relax, friction, margin, max_speed, damping, lrs, bend_compliance;
     int32_t self_collision;
+    int32_t grid_res;        // >= 1: one grid cloth of (grid_res+1)^2 particles, implicit topology
+    int32_t grid_slot_begin, grid_slot_count;  // its LRA slots (global slot indices)
     int32_t pad_[3];
 };
+
+// Grid tile: a TA x TB block of one grid cloth's particles, rows a in [a0, a0+TA),
+// columns b in [b0, b0+TB) of VertexAt(a, b) = a * (res+1) + b.
+struct GridTile {
+    int32_t dom, a0, b0, pad_;
+};
+constexpr int kGridTA = 7, kGridTB = 31;  // generators (TA+1) x (TB+1) = 8 x 32 = 256
 
 // One collider on the device: the reference's SDFCollider with VelocityAt's matrix
 // product lastTransform * invCurTransform precomputed (same arithmetic, once per frame).
@@ -87,7 +96,11 @@ struct DeviceArrays {
     // tables
     DomainParams* dom = nullptr;
     ColliderDev* col = nullptr;
-    Tile *ptiles = nullptr, *btiles = nullptr;
+    // ptiles: every domain's particles (per-particle kernels); stiles / btiles: particles
+    // and bends of the domains solved by the CSR kernels; gtiles: 2-D tiles of the grid
+    // domains solved by the implicit-topology kernel
+    Tile *ptiles = nullptr, *stiles = nullptr, *btiles = nullptr;
+    GridTile* gtiles = nullptr;
     int32_t* status = nullptr;  // device-side fault flag
 };
 
@@ -98,7 +111,12 @@ struct Launch {
     int32_t n_ptiles, n_btiles;
     int32_t n_particles;
     cudaStream_t st;
+    int32_t n_stiles = 0, n_gtiles = 0;
 };
+
+// One Jacobi iteration of the grid domains (stretch + attach + bending + ApplyDeltas,
+// optionally Finalize / Predict) with implicit topology and shared-memory tiles.
+cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int final_mode);
 
 cudaError_t launch_presdf_predict(const Launch& L, int pcur);
 cudaError_t launch_collide(const Launch& L, int pin, int pout);
