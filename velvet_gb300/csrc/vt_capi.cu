@@ -403,7 +403,16 @@ vt_status vt_cloth_build_grid_constraints(vt_solver* s, int32_t offset, int32_t 
     if (grid_candidate) {
         // bending must be one constraint per quad (x, y), in x-major order, over
         // ((x,y), (x+1,y+1), (x,y+1), (x+1,y)): true for GenerateClothMesh's triangles
-        bool ok = (int64_t)h.nbend() == (int64_t)res * res;
+        bool ok = (int64_t)h.nbend() == (int64_t)res * res && (int64_t)ni == 6ll * res * res;
+        // triangles must be GenerateClothMesh's (Velvet/Scene.hpp:153-165): the normals
+        // kernel of grid domains enumerates them implicitly
+        for (int32_t xq = 0; ok && xq < res; ++xq)
+            for (int32_t yq = 0; ok && yq < res; ++yq) {
+                const uint32_t* t = ind + 6 * ((size_t)xq * res + yq);
+                ok = t[0] == (uint32_t)VAT(xq, yq) && t[1] == (uint32_t)VAT(xq + 1, yq) &&
+                     t[2] == (uint32_t)VAT(xq, yq + 1) && t[3] == (uint32_t)VAT(xq, yq + 1) &&
+                     t[4] == (uint32_t)VAT(xq + 1, yq) && t[5] == (uint32_t)VAT(xq + 1, yq + 1);
+            }
         for (int32_t xq = 0; ok && xq < res; ++xq)
             for (int32_t yq = 0; ok && yq < res; ++yq) {
                 const uint32_t* q = &h.bd_idx[4 * ((size_t)xq * res + yq)];

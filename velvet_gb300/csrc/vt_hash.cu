@@ -336,6 +336,81 @@ k_cache_neighbors_f3(const uint32_t* __restrict__ vals, const uint32_t* __restri
                         sp, sp2, diam2, max_nbr);
 }
 
+// ------------------------------------------------------------------ arena form
+// The served form keeps each admitted cloth in a range of a sparse particle arena: a
+// per-particle domain id (negative for a free slot) replaces the tile -> domain map.
+// Free slots get a sentinel key that sorts after every cell, so the first n_active
+// sorted entries are the live particles; a domain's particles still sort by (its cell,
+// particle index), the order they have when the cloth is simulated alone.
+__global__ void __launch_bounds__(kBlock)
+k_hash_keys_arena(const int32_t* __restrict__ pdom, const DomainParams* __restrict__ doms,
+                  const float4* __restrict__ p, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                  int32_t hw, uint32_t sentinel)
+{
+    const int i = blockIdx.x * kBlock + (int)threadIdx.x;
+    if (i >= hw) return;
+    const int d = pdom[i];
+    uint32_t key = sentinel;
+    if (d >= 0) {
+        const DomainParams& D = doms[d];
+        const float4 q = p[i];
+        const float sp = D.cell_spacing;
+        key = (uint32_t)D.table_base +
+              hash_coords(int_coord(q.x, sp), int_coord(q.y, sp), int_coord(q.z, sp), D.table_size);
+    }
+    keys[i] = key;
+    vals[i] = (uint32_t)i;
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_cell_ranges_arena(const uint32_t* __restrict__ keys, int32_t n, uint32_t sentinel,
+                    uint32_t* __restrict__ cs, uint32_t* __restrict__ ce)
+{
+    const int t = blockIdx.x * kBlock + (int)threadIdx.x;
+    if (t >= n) return;
+    const uint32_t h = keys[t];
+    if (h == sentinel) return;
+    if (t == 0 || keys[t - 1] != h) {
+        cs[h] = (uint32_t)t;
+        if (t > 0) ce[keys[t - 1]] = (uint32_t)t;
+    }
+    if (t == n - 1 || keys[t + 1] == sentinel) ce[h] = (uint32_t)(t + 1);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_cache_neighbors_arena(const int32_t* __restrict__ pdom, const DomainParams* __restrict__ doms,
+                        const uint32_t* __restrict__ vals, const uint32_t* __restrict__ cs,
+                        const uint32_t* __restrict__ ce, const float4* __restrict__ p,
+                        const float4* __restrict__ x0, uint32_t* __restrict__ nbr, int32_t n_active)
+{
+    const int t = blockIdx.x * kBlock + (int)threadIdx.x;
+    if (t >= n_active) return;
+    const DomainParams& D = doms[pdom[vals[t]]];
+    cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF4{p}, PosF4{x0}, nbr + D.nbr_base,
+                        (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
+                        D.cell_spacing, D.cell_spacing2, D.diameter2, D.max_nbr);
+}
+
+cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pin, int32_t hw,
+                              int32_t n_active, uint32_t sentinel, int32_t bits, cudaStream_t st,
+                              uint64_t* launches)
+{
+    if (hw <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d.cell_start, 0xff, sizeof(uint32_t) * (size_t)sentinel, st);
+    if (e != cudaSuccess) return e;
+    const int blocks = (hw + kBlock - 1) / kBlock;
+    k_hash_keys_arena<<<blocks, kBlock, 0, st>>>(pdom, d.dom, d.p[pin], d.keys, d.vals, hw, sentinel);
+    e = radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot, hw, bits, st);
+    if (e != cudaSuccess) return e;
+    k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, hw, sentinel, d.cell_start, d.cell_end);
+    if (n_active > 0)
+        k_cache_neighbors_arena<<<(n_active + kBlock - 1) / kBlock, kBlock, 0, st>>>(
+            pdom, d.dom, d.vals, d.cell_start, d.cell_end, d.p[pin], d.x0, d.nbr, n_active);
+    const int passes = (hw > 1 && bits > 0) ? (bits + 7) / 8 : 0;
+    if (launches) *launches += 3 + 3 * (uint64_t)passes;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_hash_keys(const Launch& L, int pin)
 {
     if (!L.n_ptiles) return cudaSuccess;

@@ -126,7 +126,7 @@ public:
     std::vector<float4> hslots;
     int32_t n_domains = 0, n_particles = 0, n_bends = 0, n_slots = 0, n_cols = 0;
     int32_t total_keys = 0, n_ptiles = 0, n_btiles = 0, nbr_words = 0;
-    int32_t n_stiles = 0, n_gtiles = 0;
+    int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
     int32_t pcur = 0;  // which of p[0], p[1] holds the latest predicted positions
     uint64_t bytes = 0;
     uint64_t launches = 0;  // kernels enqueued so far

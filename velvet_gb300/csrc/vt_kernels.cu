@@ -198,11 +198,11 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
 
 // ------------------------------------------------------------------ constraint math
 // One dihedral bending constraint, SolveBending_Kernel (VtClothSolverGPU.cu:117-189).
-// a0..a3: predicted positions with the inverse mass in w.  Writes the four corrections
+// a0..a3: predicted positions with the inverse mass in w; xpbd = bendCompliance / dt / dt
+// (evaluated once per frame on the host, in that order).  Writes the four corrections
 // with w = 1 when the constraint fired, all zero when it returned early.
 __device__ __forceinline__ void bend_eval(float4 a0, float4 a1, float4 a2, float4 a3, float rest,
-                                          float bend_compliance, float dt, float4& c0, float4& c1,
-                                          float4& c2, float4& c3)
+                                          float xpbd, float4& c0, float4& c1, float4& c2, float4& c3)
 {
     const vec3 p0 = xyz(a0), p1 = xyz(a1), p2 = xyz(a2), p3 = xyz(a3);
     const float w0 = a0.w, w1 = a1.w, w2 = a2.w, w3 = a3.w;
@@ -229,7 +229,6 @@ __device__ __forceinline__ void bend_eval(float4 a0, float4 a1, float4 a2, float
     lambda = lambda + w2 * dot(d2, d2);
     lambda = lambda + w3 * dot(d3, d3);
     if (lambda < VT_EPSILON) return;
-    const float xpbd = bend_compliance / dt / dt;
     lambda = (phi - rest) / (lambda + xpbd);
     if (dot(cross(n1, n2), e) > 0.0f) lambda = -lambda;
     const vec3 k0 = d0 * (-w0 * lambda), k1 = d1 * (-w1 * lambda);
@@ -319,7 +318,7 @@ k_bend(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
     const DomainParams& D = doms[tl.dom];
     const uint4 q = bidx[b];
     float4 c0, c1, c2, c3;
-    bend_eval(pin[q.x], pin[q.y], pin[q.z], pin[q.w], brest[b], D.bend_compliance, D.dt_sub, c0, c1, c2, c3);
+    bend_eval(pin[q.x], pin[q.y], pin[q.z], pin[q.w], brest[b], D.xpbd_bend, c0, c1, c2, c3);
     float4* out = bcorr + 4 * (size_t)b;
     out[0] = c0;
     out[1] = c1;
@@ -396,22 +395,26 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
 // (x, y) over ((x,y), (x+1,y+1), (x,y+1), (x+1,y)) (:118-132), rest lengths
 // |x0_i - x0_j| (the builder's values: registration verifies x == x0 at build time)
 // and rest angles 0.  A block owns a 7 x 31 tile; it stages the tile and a one-particle
-// halo of predicted and initial positions in shared memory, evaluates each of the
-// 8 x 32 generators touching the tile once (one per thread: one bend + four stretch
+// halo of predicted positions in shared memory, evaluates each of the 8 x 32
+// generators touching the tile once (one per thread: one bend + four stretch
 // constraints), then each particle sums its eight stretch, the LRA and its four bending
 // corrections in constraint order — the order of the CSR kernel and of the oracle.
+// The rest lengths |x0_i - x0_j| of a generator's four constraints (grest) and a
+// particle's LRA rest distances (glra, up to kGridLraCached slots) are evaluated once
+// at registration with the same FP32 operations instead of every iteration: the kernel
+// is bound by instruction issue, HBM is mostly idle.
 constexpr int kGHA = kGridTA + 2, kGHB = kGridTB + 2;  // halo tile 9 x 33
 constexpr int kGGA = kGridTA + 1, kGGB = kGridTB + 1;  // generators 8 x 32
 
 template <int kMode>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 4)
 k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__ doms,
             const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ x,
-            float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ slots,
+            float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ grest,
+            const float4* __restrict__ glra, const float4* __restrict__ slots,
             const float4* __restrict__ slots0, int32_t* __restrict__ status)
 {
     __shared__ float4 sp[kGHA][kGHB];
-    __shared__ float4 sx0[kGHA][kGHB];
     __shared__ float4 sst[4][kGGA][kGGB];  // stretch common + fired flag, per type
     __shared__ float4 sbd[4][kGGA][kGGB];  // bending corner corrections + fired flag
     const GridTile tl = tiles[blockIdx.x];
@@ -420,18 +423,13 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     const int a0 = tl.a0, b0 = tl.b0;
     const int tid = (int)threadIdx.x;
 
-    // 1. halo tile of predicted and initial positions
+    // 1. halo tile of predicted positions
     for (int k = tid; k < kGHA * kGHB; k += kBlock) {
         const int ha = k / kGHB, hb = k - ha * kGHB;
         const int a = a0 - 1 + ha, b = b0 - 1 + hb;
-        float4 q = make_float4(0, 0, 0, 0), o = q;
-        if (a >= 0 && a < V && b >= 0 && b < V) {
-            const int i = base + a * V + b;
-            q = pin[i];
-            o = x0[i];
-        }
+        float4 q = make_float4(0, 0, 0, 0);
+        if (a >= 0 && a < V && b >= 0 && b < V) q = pin[base + a * V + b];
         sp[ha][hb] = q;
-        sx0[ha][hb] = o;
     }
     __syncthreads();
 
@@ -444,27 +442,23 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
         float4 c0 = zero, c1 = zero, c2 = zero, c3 = zero;
         if (X >= 0 && Y >= 0 && X <= R && Y <= R) {
             const float4 pxy = sp[gx][gy];
-            const vec3 oxy = xyz(sx0[gx][gy]);
+            const float4 rest = grest[base + X * V + Y];
             vec3 cm;
             if (Y < R) {  // t0: (x,y)-(x,y+1)
-                if (stretch_common(pxy, sp[gx][gy + 1], length(oxy - xyz(sx0[gx][gy + 1])), cm))
-                    s0 = make_float4(cm.x, cm.y, cm.z, 1.0f);
+                if (stretch_common(pxy, sp[gx][gy + 1], rest.x, cm)) s0 = make_float4(cm.x, cm.y, cm.z, 1.0f);
             }
             if (X < R) {  // t1: (x,y)-(x+1,y)
-                if (stretch_common(pxy, sp[gx + 1][gy], length(oxy - xyz(sx0[gx + 1][gy])), cm))
-                    s1 = make_float4(cm.x, cm.y, cm.z, 1.0f);
+                if (stretch_common(pxy, sp[gx + 1][gy], rest.y, cm)) s1 = make_float4(cm.x, cm.y, cm.z, 1.0f);
             }
             if (X < R && Y < R) {
                 // t2: (x,y)-(x+1,y+1)
-                if (stretch_common(pxy, sp[gx + 1][gy + 1], length(oxy - xyz(sx0[gx + 1][gy + 1])), cm))
-                    s2 = make_float4(cm.x, cm.y, cm.z, 1.0f);
+                if (stretch_common(pxy, sp[gx + 1][gy + 1], rest.z, cm)) s2 = make_float4(cm.x, cm.y, cm.z, 1.0f);
                 // t3: (x,y+1)-(x+1,y)
-                if (stretch_common(sp[gx][gy + 1], sp[gx + 1][gy],
-                                   length(xyz(sx0[gx][gy + 1]) - xyz(sx0[gx + 1][gy])), cm))
+                if (stretch_common(sp[gx][gy + 1], sp[gx + 1][gy], rest.w, cm))
                     s3 = make_float4(cm.x, cm.y, cm.z, 1.0f);
                 // bend of quad (x, y): corners (x,y), (x+1,y+1), (x,y+1), (x+1,y)
-                bend_eval(pxy, sp[gx + 1][gy + 1], sp[gx][gy + 1], sp[gx + 1][gy], 0.0f,
-                          D.bend_compliance, D.dt_sub, c0, c1, c2, c3);
+                bend_eval(pxy, sp[gx + 1][gy + 1], sp[gx][gy + 1], sp[gx + 1][gy], 0.0f, D.xpbd_bend,
+                          c0, c1, c2, c3);
             }
         }
         sst[0][gx][gy] = s0;
@@ -510,10 +504,19 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
 #undef VT_TAKE
     // long-range attachments, slot order
     if (D.grid_slot_count) {
-        const vec3 x0i = xyz(sx0[gx][gy]);
-        for (int s = D.grid_slot_begin; s < D.grid_slot_begin + D.grid_slot_count; ++s) {
-            const float rest = length(xyz(slots0[s]) - x0i);
-            attach_one(pi, wi, xyz(slots[s]), rest * D.lrs, acc, cnt);
+        const int s0 = D.grid_slot_begin, ns = D.grid_slot_count;
+        if (ns <= kGridLraCached) {
+            const float4 r4 = glra[i];
+            const float rs[4] = {r4.x, r4.y, r4.z, r4.w};
+#pragma unroll
+            for (int k = 0; k < kGridLraCached; ++k)
+                if (k < ns) attach_one(pi, wi, xyz(slots[s0 + k]), rs[k] * D.lrs, acc, cnt);
+        } else {
+            const vec3 x0i = xyz(x0[i]);
+            for (int s = s0; s < s0 + ns; ++s) {
+                const float rest = length(xyz(slots0[s]) - x0i);
+                attach_one(pi, wi, xyz(slots[s]), rest * D.lrs, acc, cnt);
+            }
         }
     }
     // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
@@ -587,6 +590,41 @@ k_normals(const Tile* __restrict__ tiles, const float4* __restrict__ x,
     nrm[i] = make_float4(n.x, n.y, n.z, 0.0f);
 }
 
+// Normals of a grid cloth with GenerateClothMesh's triangles, enumerated implicitly:
+// quad (x, y) holds triangles 2q = ((x,y), (x+1,y), (x,y+1)) and 2q+1 = ((x,y+1),
+// (x+1,y), (x+1,y+1)), q = x*R + y (Velvet/Scene.hpp:153-165).  Vertex (a, b) sums its
+// incident triangles in triangle order — (a-1,b-1).1, (a-1,b).0, (a-1,b).1, (a,b-1).0,
+// (a,b-1).1, (a,b).0 — as the CSR kernel and the reference's serialised atomics do.
+__global__ void __launch_bounds__(kBlock)
+k_grid_normals(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+               const float4* __restrict__ x, float4* __restrict__ nrm)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int i = tl.begin + (int)threadIdx.x;
+    if (i >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    const int R = D.grid_res, V = R + 1, base = D.p_begin;
+    const int li = i - base, a = li / V, b = li - a * V;
+    auto P = [&](int aa, int bb) { return xyz(x[base + aa * V + bb]); };
+    auto tri_n = [&](int a1, int b1, int a2, int b2, int a3, int b3) {
+        const vec3 p1 = P(a1, b1), p2 = P(a2, b2), p3 = P(a3, b3);
+        return cross(p2 - p1, p3 - p1);
+    };
+    vec3 acc = mk3(0, 0, 0);
+    if (a >= 1 && b >= 1) acc3(acc, tri_n(a - 1, b, a, b - 1, a, b));              // (a-1,b-1).1
+    if (a >= 1 && b < R) {
+        acc3(acc, tri_n(a - 1, b, a, b, a - 1, b + 1));                               // (a-1,b).0
+        acc3(acc, tri_n(a - 1, b + 1, a, b, a, b + 1));                               // (a-1,b).1
+    }
+    if (a < R && b >= 1) {
+        acc3(acc, tri_n(a, b - 1, a + 1, b - 1, a, b));                               // (a,b-1).0
+        acc3(acc, tri_n(a, b, a + 1, b - 1, a + 1, b));                               // (a,b-1).1
+    }
+    if (a < R && b < R) acc3(acc, tri_n(a, b, a + 1, b, a, b + 1));                 // (a,b).0
+    const vec3 n = normalize(acc);
+    nrm[i] = make_float4(n.x, n.y, n.z, 0.0f);
+}
+
 // ------------------------------------------------------------------ launchers
 cudaError_t launch_presdf_predict(const Launch& L, int pcur)
 {
@@ -629,11 +667,26 @@ cudaError_t launch_solve(const Launch& L, int pin, int pout, int mode)
     return cudaGetLastError();
 }
 
+cudaError_t prepare_kernels()
+{
+    // most shared memory per SM for the tile kernel: more resident tiles per SM
+    cudaError_t e = cudaFuncSetAttribute(k_grid_iter<SOLVE_PLAIN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_grid_iter<SOLVE_FINALIZE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_grid_iter<SOLVE_FINALIZE_PREDICT>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    return e;
+}
+
 cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int mode)
 {
     if (!L.n_gtiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
-#define VT_GRID_ARGS d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.slots, d.slots0, d.status
+#define VT_GRID_ARGS \
+    d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.grest, d.glra, d.slots, d.slots0, d.status
     if (mode == SOLVE_PLAIN)
         k_grid_iter<SOLVE_PLAIN><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
     else if (mode == SOLVE_FINALIZE)
@@ -657,9 +710,9 @@ cudaError_t launch_finalize(const Launch& L, int pcur, int predict_next)
 
 cudaError_t launch_normals(const Launch& L)
 {
-    if (!L.n_ptiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
-    k_normals<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.x, d.tri, d.tn_off, d.tn_ent, d.nrm);
+    if (L.n_stiles) k_normals<<<L.n_stiles, kBlock, 0, L.st>>>(d.stiles, d.x, d.tri, d.tn_off, d.tn_ent, d.nrm);
+    if (L.n_gptiles) k_grid_normals<<<L.n_gptiles, kBlock, 0, L.st>>>(d.gptiles, d.dom, d.x, d.nrm);
     return cudaGetLastError();
 }
 

@@ -306,8 +306,9 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     at.init(N);
     bd.init(N);
     tn.init(N);
-    std::vector<Tile> pt, st_tiles, bt;
+    std::vector<Tile> pt, st_tiles, bt, gpt;
     std::vector<GridTile> gt;
+    std::vector<float4> hgrest(N, make_float4(0, 0, 0, 0)), hglra(N, make_float4(0, 0, 0, 0));
     hdom.assign(n_domains, DomainParams{});
     hcol.clear();
 
@@ -317,11 +318,11 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         int32_t p0 = 0;
         for (size_t k = 0; k < S.size(); ++k) {
             const HostSolver* h = S[k];
-            for (size_t q = 0; q < h->tri.size() / 3 * 3; ++q) tn.count(p0 + (int32_t)h->tri[q]);
             if (grid[k]) {
                 p0 += (int32_t)h->n();
                 continue;
             }
+            for (size_t q = 0; q < h->tri.size() / 3 * 3; ++q) tn.count(p0 + (int32_t)h->tri[q]);
             for (size_t c = 0; c < h->st_rest.size(); ++c) {
                 st.count(p0 + h->st_idx[2 * c]);
                 st.count(p0 + h->st_idx[2 * c + 1]);
@@ -390,7 +391,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         for (int32_t t = 0; t < ntri; ++t) {
             const uint32_t* q = &h.tri[3 * t];
             htri[tb + t] = make_uint4(pb + q[0], pb + q[1], pb + q[2], 0);
-            for (int j = 0; j < 3; ++j) tn.put(pb + (int32_t)q[j], tb + t);
+            for (int j = 0; !g && j < 3; ++j) tn.put(pb + (int32_t)q[j], tb + t);
         }
         for (const vt_sdf_collider& c : h.colliders) hcol.push_back(collider_to_device(c));
 
@@ -410,9 +411,34 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
             D.grid_res = h.grid_res;
             D.grid_slot_begin = sb + h.grid_slot_begin;
             D.grid_slot_count = h.grid_slot_count;
-            const int32_t V = h.grid_res + 1;
+            const int32_t R = h.grid_res, V = R + 1;
+            // rest lengths per generator, read from the constraint list in its order
+            size_t c = 0;
+            for (int32_t X = 0; X <= R; ++X)
+                for (int32_t Y = 0; Y <= R; ++Y) {
+                    float r[4] = {0, 0, 0, 0};
+                    if (Y != R) r[0] = h.st_rest[c++];
+                    if (X != R) r[1] = h.st_rest[c++];
+                    if (X != R && Y != R) {
+                        r[2] = h.st_rest[c++];
+                        r[3] = h.st_rest[c++];
+                    }
+                    hgrest[pb + X * V + Y] = make_float4(r[0], r[1], r[2], r[3]);
+                }
+            // LRA rest distances |slot0 - x0_i| of the first slots
+            const int32_t ns = std::min(h.grid_slot_count, kGridLraCached);
+            for (int32_t i = 0; i < n; ++i) {
+                float r[4] = {0, 0, 0, 0};
+                const vec3 xi = mk3(h.x0[3 * i], h.x0[3 * i + 1], h.x0[3 * i + 2]);
+                for (int32_t s = 0; s < ns; ++s) {
+                    const float* q = &h.slots0[3 * (size_t)(h.grid_slot_begin + s)];
+                    r[s] = length(mk3(q[0], q[1], q[2]) - xi);
+                }
+                hglra[pb + i] = make_float4(r[0], r[1], r[2], r[3]);
+            }
             for (int32_t a = 0; a < V; a += kGridTA)
                 for (int32_t b = 0; b < V; b += kGridTB) gt.push_back(GridTile{k, a, b, 0});
+            tiles_for(gpt, k, pb, n);
         } else {
             D.grid_res = 0;
             tiles_for(st_tiles, k, pb, n);
@@ -431,6 +457,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     n_btiles = (int32_t)bt.size();
     n_stiles = (int32_t)st_tiles.size();
     n_gtiles = (int32_t)gt.size();
+    n_gptiles = (int32_t)gpt.size();
     hslots = hslot;
 
     // ---- device arena
@@ -451,6 +478,9 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_dom = A.take<DomainParams>(n_domains), o_col = A.take<ColliderDev>(C);
     const size_t o_pt = A.take<Tile>(pt.size()), o_bt = A.take<Tile>(bt.size());
     const size_t o_stt = A.take<Tile>(st_tiles.size()), o_gt = A.take<GridTile>(gt.size());
+    const size_t o_gpt = A.take<Tile>(gpt.size());
+    const bool any_grid = !gt.empty();
+    const size_t o_grest = A.take<float4>(any_grid ? N : 0), o_glra = A.take<float4>(any_grid ? N : 0);
     const size_t o_st = A.take<int32_t>(1 + n_domains);
     bytes = A.off;
     VT_CUDA(cudaMalloc(&arena_, A.off), "cudaMalloc(world)");
@@ -470,7 +500,8 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     d.cell_start = AT(uint32_t, o_cs); d.cell_end = AT(uint32_t, o_ce); d.nbr = AT(uint32_t, o_nb);
     d.dom = AT(DomainParams, o_dom); d.col = AT(ColliderDev, o_col);
     d.ptiles = AT(Tile, o_pt); d.btiles = AT(Tile, o_bt); d.status = AT(int32_t, o_st);
-    d.stiles = AT(Tile, o_stt); d.gtiles = AT(GridTile, o_gt);
+    d.stiles = AT(Tile, o_stt); d.gtiles = AT(GridTile, o_gt); d.gptiles = AT(Tile, o_gpt);
+    d.grest = AT(float4, o_grest); d.glra = AT(float4, o_glra);
 #undef AT
     auto up = [](void* dst, const void* src, size_t bytes_) -> cudaError_t {
         return bytes_ ? cudaMemcpy(dst, src, bytes_, cudaMemcpyHostToDevice) : cudaSuccess;
@@ -502,6 +533,12 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     VT_CUDA(up(d.btiles, bt.data(), bt.size() * sizeof(Tile)), "upload btiles");
     VT_CUDA(up(d.stiles, st_tiles.data(), st_tiles.size() * sizeof(Tile)), "upload stiles");
     VT_CUDA(up(d.gtiles, gt.data(), gt.size() * sizeof(GridTile)), "upload gtiles");
+    VT_CUDA(up(d.gptiles, gpt.data(), gpt.size() * sizeof(Tile)), "upload gptiles");
+    if (any_grid) {
+        VT_CUDA(up(d.grest, hgrest.data(), N * 16), "upload grest");
+        VT_CUDA(up(d.glra, hglra.data(), N * 16), "upload glra");
+    }
+    VT_CUDA(prepare_kernels(), "kernel attributes");
     VT_CUDA(cudaMemset(d.status, 0, (1 + n_domains) * 4), "memset status");
 
     staging_bytes_ = sizeof(DomainParams) * n_domains + sizeof(ColliderDev) * C + 16 * SL + 64;
@@ -533,6 +570,7 @@ void World::set_frame(int k, const HostSolver& h, const FrameArgs& a)
     D.damping = P.damping;
     D.lrs = P.long_range_stretchiness;
     D.bend_compliance = P.bend_compliance;
+    D.xpbd_bend = P.bend_compliance / D.dt_sub / D.dt_sub;  // SolveBending_Kernel's xpbd_bend
     D.self_collision = P.enable_self_collision ? 1 : 0;
 }
 
@@ -642,7 +680,7 @@ vt_status World::upload_frame(cudaStream_t st)
 
 vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cudaStream_t st)
 {
-    Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles};
+    Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles, n_gptiles};
     int pc = 0;
     int bits = 0;
     while ((1ll << bits) < (int64_t)total_keys) ++bits;

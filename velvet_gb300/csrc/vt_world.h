@@ -44,8 +44,12 @@ struct DomainParams {
     int32_t self_collision;
     int32_t grid_res;        // >= 1: one grid cloth of (grid_res+1)^2 particles, implicit topology
     int32_t grid_slot_begin, grid_slot_count;  // its LRA slots (global slot indices)
-    int32_t pad_[3];
+    float xpbd_bend;         // bend_compliance / dt_sub / dt_sub, evaluated in that order
+    int32_t pad_[2];
 };
+
+// Most LRA slots per grid cloth whose rest distances are precomputed per particle.
+constexpr int kGridLraCached = 4;
 
 // Grid tile: a TA x TB block of one grid cloth's particles, rows a in [a0, a0+TA),
 // columns b in [b0, b0+TB) of VertexAt(a, b) = a * (res+1) + b.
@@ -89,6 +93,9 @@ struct DeviceArrays {
     uint4* bd_idx = nullptr; float* bd_rest = nullptr; float4* bd_corr = nullptr;
     int32_t *bd_off = nullptr, *bd_ent = nullptr;
     uint4* tri = nullptr; int32_t *tn_off = nullptr, *tn_ent = nullptr;
+    // grid domains: rest lengths of the four stretch constraints generator (a, b) owns
+    // (t0..t3, |x0_i - x0_j|), and the LRA rest distances of up to four slots
+    float4 *grest = nullptr, *glra = nullptr;
     // hash
     uint32_t *keys = nullptr, *vals = nullptr, *keys_tmp = nullptr, *vals_tmp = nullptr;
     uint32_t *hist = nullptr, *digit_tot = nullptr;
@@ -100,6 +107,7 @@ struct DeviceArrays {
     // and bends of the domains solved by the CSR kernels; gtiles: 2-D tiles of the grid
     // domains solved by the implicit-topology kernel
     Tile *ptiles = nullptr, *stiles = nullptr, *btiles = nullptr;
+    Tile* gptiles = nullptr;  // particles of the grid domains (normals)
     GridTile* gtiles = nullptr;
     int32_t* status = nullptr;  // device-side fault flag
 };
@@ -111,12 +119,14 @@ struct Launch {
     int32_t n_ptiles, n_btiles;
     int32_t n_particles;
     cudaStream_t st;
-    int32_t n_stiles = 0, n_gtiles = 0;
+    int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
 };
 
 // One Jacobi iteration of the grid domains (stretch + attach + bending + ApplyDeltas,
 // optionally Finalize / Predict) with implicit topology and shared-memory tiles.
 cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int final_mode);
+// One-time kernel attributes (call outside any stream capture).
+cudaError_t prepare_kernels();
 
 cudaError_t launch_presdf_predict(const Launch& L, int pcur);
 cudaError_t launch_collide(const Launch& L, int pin, int pout);
@@ -139,6 +149,11 @@ size_t radix_hist_words(int32_t n);  // size of `hist` for n items
 cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_start,
                                uint32_t* cell_end, cudaStream_t st);
 cudaError_t launch_cache_neighbors(const Launch& L, int pin);
+// Spatial hash of a sparse particle arena (the served form): particles [0, hw) with
+// per-particle domain ids pdom (< 0: free); cells [0, sentinel); n_active live particles.
+cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pin, int32_t hw,
+                              int32_t n_active, uint32_t sentinel, int32_t bits, cudaStream_t st,
+                              uint64_t* launches);
 // HashObjects on float3 caller buffers (vt_hash_objects); scratch supplied by the caller:
 // keys_tmp / vals_tmp num_objects words each, hist radix_hist_words(num_objects),
 // digit_tot 256 words.
