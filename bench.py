@@ -192,6 +192,27 @@ def cpu_baseline_single(wl_name: str, seed: int, budget_s: float = 15.0) -> dict
                       f"{frames} frame(s), {pits / 1e6:.1f} M particle-iterations in {secs:.1f} s"}
 
 
+def cpu_reference_solver_single(budget_s: float = 8.0) -> dict:
+    """The reference's own CPU solver (VtClothSolverCPU, restated in oracle/vt_cpu_solver.c:
+    a different, Gauss-Seidel algorithm) on one core, on its own CPU configuration: one
+    64x64 cloth, 5 substeps x 10 iterations."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle import CpuSolver
+    from velvet_gb300 import workloads as W
+
+    wl = W.small()
+    s = CpuSolver(wl.cloths[0])
+    frames, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and frames < 300:
+        s.simulate(float(W.FRAME_DT), wl.substeps, wl.iterations)
+        frames += 1
+    secs = time.perf_counter() - t0
+    s.close()
+    pits = wl.num_particles * wl.substeps * wl.iterations * frames
+    return {"value": pits / secs, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"VtClothSolverCPU restated: 64x64 cloth, {frames} frames in {secs:.1f} s"}
+
+
 def run_reference(args) -> None:
     rank, world, _ = env_rank()
     if rank != 0:
@@ -338,6 +359,115 @@ def pct(v, q):
     return s[min(len(s) - 1, int(q * len(s)))]
 
 
+def run_serving(args) -> None:
+    """Served form: Poisson arrivals (--rate req/s for --duration s), each request one
+    grid cloth with side log-uniform in [16, 512] and a frame count uniform in [30, 300],
+    admitted by the HBM budget (--budget-gb) and an active-particle cap, one frame for all
+    active requests per tick.  Requests wait in a front-end backlog and enter the
+    server's queue as it drains.  Reports aggregate particle-iterations/s over the wall
+    time, p50/p99 frame latency, and the plain solver run one request at a time on the
+    same arrival stream for a bounded time."""
+    import torch
+
+    import velvet_gb300 as vg
+    from velvet_gb300 import workloads as W
+
+    rng = np.random.default_rng(args.seed)
+    n_req = int(args.rate * args.duration * 1.5) + 16
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
+    sides = np.rint(np.exp(rng.uniform(math.log(16), math.log(512), n_req))).astype(int)
+    frames = rng.integers(30, 301, n_req)
+    S, It = 5, 10
+    templates: dict[int, object] = {}
+
+    def template(side):
+        if side not in templates:
+            spec = W.ClothSpec(side, 0.02, W.horizontal_cloth(side, 0.02, 0.8), [0, side - 1],
+                               W.static_colliders([W.sphere((0.0, 0.3, 0.0), 0.3), W.plane(0.0)]))
+            s = vg.ClothSolver()
+            W.build_plain(spec, s)
+            templates[side] = (s, spec)
+        return templates[side]
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    srv = vg.ClothServer(int(args.budget_gb * (1 << 30)), max_cloths=4096,
+                         max_active_particles=args.max_active_particles, substeps=S, iterations=It)
+    # warm-up: one small request through the whole path
+    s0, _ = template(16)
+    srv.submit(s0, 3)
+    while srv.tick(stream).active or srv.stats().requests_done < 1:
+        pass
+    base = srv.stats()
+    k = 0
+    backlog: list[int] = []
+    ticks, admitted, active_samples = 0, 0, []
+    t0 = time.perf_counter()
+    while True:
+        now = time.perf_counter() - t0
+        if now >= args.duration:
+            break
+        while k < n_req and arrivals[k] <= now:
+            backlog.append(k)
+            k += 1
+        info_q = 0
+        while backlog and info_q < 2:
+            j = backlog.pop(0)
+            s, _ = template(int(sides[j]))
+            srv.submit(s, int(frames[j]))
+            info_q += 1
+        info = srv.tick(stream)
+        ticks += 1
+        admitted += info.admitted
+        active_samples.append(info.active_particles)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    pits = st.particle_iterations - base.particle_iterations
+    served = {"value": pits / wall, "unit": UNIT, "wall_s": wall, "ticks": ticks,
+              "p50_frame_ms": st.p50_frame_ms, "p99_frame_ms": st.p99_frame_ms,
+              "arrived": k, "admitted": admitted, "completed": int(st.requests_done - base.requests_done),
+              "backlog_at_end": len(backlog),
+              "mean_active_particles": float(np.mean(active_samples)) if active_samples else 0.0,
+              "gpu_busy_frac": (st.gpu_ms - base.gpu_ms) / 1000.0 / wall}
+    srv.close()
+
+    # the plain solver, one request at a time, same stream of requests, bounded time
+    p_pits, p_frames, p_ms = 0, [], 0.0
+    t1 = time.perf_counter()
+    j = 0
+    while time.perf_counter() - t1 < args.plain_seconds and j < n_req:
+        _, spec = template(int(sides[j]))
+        s = vg.ClothSolver()
+        W.build_plain(spec, s)
+        d = spec.particle_diameter()
+        for f in range(int(frames[j])):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.simulate(float(W.FRAME_DT), S, It, 1.0, 0.1, 0.06, d, stream)
+            e1.record(stream)
+            e1.synchronize()
+            p_frames.append(e0.elapsed_time(e1))
+            p_pits += spec.num_particles * S * It
+            if time.perf_counter() - t1 >= args.plain_seconds:
+                break
+        s.close()
+        j += 1
+    p_wall = time.perf_counter() - t1
+    plain = {"value": p_pits / p_wall, "unit": UNIT, "wall_s": p_wall, "requests": j,
+             "p50_frame_ms": statistics.median(p_frames), "p99_frame_ms": pct(p_frames, 0.99)}
+    line = {"metric": METRIC, "value": served["value"], "unit": UNIT, "n_gpus": 1, "steps": ticks,
+            "warmup": 1, "ms_per_step": 1000 * wall / max(1, ticks), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": f"synthetic Poisson request stream, seed {args.seed}",
+            "config": {"workload": "serving", "rate_per_s": args.rate, "duration_s": args.duration,
+                       "side": "log-uniform [16, 512]", "frames": "uniform [30, 300]",
+                       "budget_gb": args.budget_gb, "max_active_particles": args.max_active_particles,
+                       "substeps": S, "iterations": It},
+            "served": served, "plain": plain, "served_over_plain": served["value"] / plain["value"],
+            "p50_frame_ms": served["p50_frame_ms"], "p99_frame_ms": served["p99_frame_ms"]}
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -352,6 +482,13 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain solver")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="only run this many frames of the workload and exit (for ncu captures)")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of arrivals")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device-memory budget")
+    ap.add_argument("--max-active-particles", type=int, default=2_500_000,
+                    help="serving: admission stops above this many active particles")
+    ap.add_argument("--plain-seconds", type=float, default=15.0,
+                    help="serving: seconds of the one-request-at-a-time plain comparison")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -359,6 +496,9 @@ def main() -> None:
         return
     if args.profile_frames:
         profile_frames(args)
+        return
+    if args.workload == "serving":
+        run_serving(args)
         return
 
     import torch
@@ -472,9 +612,10 @@ def main() -> None:
         for s, _, _ in solvers:
             s.close()
 
-    cpu = None
+    cpu, cpu_ref_solver = None, None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_single(args.workload, args.seed)
+        cpu_ref_solver = cpu_reference_solver_single()
 
     if rank == 0:
         line = {
@@ -495,6 +636,7 @@ def main() -> None:
             "gpu_launches": launches_timed,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "cpu_reference_cpu_solver": cpu_ref_solver,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -298,6 +298,63 @@ vt_status vt_batch_launch_count(const vt_batch* b, uint64_t* out);
 /* Use CUDA graphs for frames (default 1); 0 launches every kernel directly. */
 vt_status vt_batch_use_graphs(vt_batch* b, int32_t on);
 
+/* ------------------------------------------------------------------ served solver
+ * Continuous batching of cloth-simulation requests (no reference counterpart).  A
+ * request is one grid cloth registered on a vt_solver with
+ * vt_cloth_build_grid_constraints, plus a number of frames.  Requests wait in a FIFO
+ * queue; each vt_server_tick first retires finished requests (their final positions are
+ * kept for vt_server_result), then admits queued requests while the device-memory
+ * budget, the slot table and the active-particle cap allow, then advances every active
+ * request by one frame with one set of multi-cloth launches.  Admitted state stays
+ * resident on the device until retirement; admission and retirement never move other
+ * requests' state.  A request's results are bit-identical to the same cloth simulated
+ * alone on a vt_solver with the server's frame arguments. */
+typedef struct vt_server vt_server;
+
+typedef struct vt_server_config {
+    uint64_t hbm_budget_bytes;     /* device memory the arena may use (admission budget)   */
+    uint32_t max_cloths;           /* active request slots                                  */
+    uint32_t max_active_particles; /* admission stops above this (0: no cap); bounds a tick */
+    float    frame_dt;             /* frame arguments shared by all requests                */
+    int32_t  substeps, iterations;
+    float    relaxation, friction, collision_margin;
+} vt_server_config;
+
+#define VT_REQ_QUEUED 0
+#define VT_REQ_ACTIVE 1
+#define VT_REQ_DONE   2
+
+typedef struct vt_server_tick_info {
+    int32_t  admitted, retired, active, queued;
+    uint64_t active_particles;
+    double   frame_ms;             /* GPU time of this tick's frame (CUDA events)           */
+} vt_server_tick_info;
+
+typedef struct vt_server_stats {
+    uint64_t ticks, frames_done, requests_done;
+    double   particle_iterations;  /* sum over ticks of active particles * substeps * iterations */
+    double   gpu_ms;               /* sum of frame_ms                                        */
+    double   p50_frame_ms, p99_frame_ms;  /* over all (request, frame) pairs                 */
+    uint64_t bytes_in_use, bytes_budget;
+} vt_server_stats;
+
+vt_status vt_server_create(const vt_server_config* cfg, vt_server** out);
+vt_status vt_server_destroy(vt_server* s);
+
+/* Queues `cloth` (copied; the solver may be destroyed afterwards) for `frames` frames.
+ * VT_ERR_CAPACITY if the request could never be admitted (larger than the budget). */
+vt_status vt_server_submit(vt_server* s, vt_solver* cloth, int32_t frames, int64_t* request_id);
+
+/* Retire, admit, one frame for every active request; waits for the frame to finish. */
+vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info);
+
+vt_status vt_server_poll(vt_server* s, int64_t request_id, int32_t* state, int32_t* frames_done);
+
+/* Final positions of a finished request (count = its particle count) into host memory. */
+vt_status vt_server_result(vt_server* s, int64_t request_id, float* dst, uint32_t count);
+
+vt_status vt_server_stats_get(vt_server* s, vt_server_stats* out);
+
 /* ------------------------------------------------------------------ profiler
  * Per-stage GPU timing, the counterpart of the reference's ScopedTimerGPU labels
  * (Velvet/Timer.hpp:95-151, 242-260): while enabled, every stage launch of every

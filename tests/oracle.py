@@ -86,6 +86,63 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
+_CL = None
+CPU_LIB = ROOT / "oracle" / "libvt_cpu_solver.so"
+
+
+def cpu_solver_lib() -> C.CDLL:
+    """oracle/libvt_cpu_solver.so: the reference's CPU solver restated (timing only)."""
+    global _CL
+    if _CL is None:
+        src = ROOT / "oracle" / "vt_cpu_solver.c"
+        if not CPU_LIB.exists() or src.stat().st_mtime > CPU_LIB.stat().st_mtime:
+            build()
+        L = C.CDLL(str(CPU_LIB))
+        P = C.c_void_p
+        L.vc_create.restype = P
+        L.vc_create.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, C.c_int, C.POINTER(VtParams)]
+        L.vc_destroy.argtypes = [P]
+        L.vc_colliders_set.argtypes = [P, P, C.c_int]
+        L.vc_simulate.argtypes = [P, C.c_float, C.c_int, C.c_int]
+        L.vc_positions.argtypes = [P, P]
+        _CL = L
+    return _CL
+
+
+class CpuSolver:
+    """The reference's CPU solver (VtClothSolverCPU) on one grid cloth: timing only."""
+
+    def __init__(self, spec, params: VtParams | None = None):
+        p = params
+        if p is None:
+            p = VtParams()
+            lib().vo_params_default(C.byref(p))
+        verts, idx = spec.mesh()
+        verts = np.ascontiguousarray(verts, np.float32)
+        idx = np.ascontiguousarray(idx, np.uint32)
+        m = colmajor(spec.model)
+        at = np.ascontiguousarray(list(spec.attached), np.int32)
+        self.n = verts.shape[0]
+        self.h = cpu_solver_lib().vc_create(_p(verts), self.n, _p(idx), idx.size, _p(m), spec.resolution,
+                                            _p(at) if at.size else None, at.size, C.byref(p))
+        cols = spec.colliders(0)
+        arr = (VtSdfCollider * max(1, len(cols)))(*cols)
+        cpu_solver_lib().vc_colliders_set(self.h, arr, len(cols))
+
+    def simulate(self, frame_dt, substeps, iterations):
+        cpu_solver_lib().vc_simulate(self.h, frame_dt, substeps, iterations)
+
+    def positions(self):
+        out = np.empty((self.n, 3), np.float32)
+        cpu_solver_lib().vc_positions(self.h, _p(out))
+        return out
+
+    def close(self):
+        if self.h:
+            cpu_solver_lib().vc_destroy(self.h)
+            self.h = None
+
+
 def colmajor(m) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(m, np.float32).T).reshape(-1)
 

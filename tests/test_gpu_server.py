@@ -1,0 +1,97 @@
+"""GPU: the served form.  Requests of different sizes arrive while others are on the
+GPU; each is admitted when a slot and memory free up, shares launches with the others,
+and must end with exactly the bits it gets when simulated alone on the plain solver."""
+import numpy as np
+import pytest
+
+import velvet_gb300 as vg
+from velvet_gb300 import _abi
+from velvet_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def request(side, height=0.6, mover=False):
+    cols = W.moving_sphere(0.2, 0.2, 1.0) if mover else W.static_colliders([W.sphere((0, 0.3, 0), 0.3), W.plane(0)])
+    return W.ClothSpec(side, 0.02, W.horizontal_cloth(side, 0.02, height), [0, side - 1], cols)
+
+
+def alone(spec, frames, S=3, It=4):
+    s = vg.ClothSolver()
+    W.build_plain(spec, s)
+    for _ in range(frames):
+        s.simulate(float(W.FRAME_DT), S, It, 1.0, 0.1, 0.06, spec.particle_diameter())
+    s.sync()
+    return s.positions()
+
+
+def registered(spec):
+    s = vg.ClothSolver()
+    W.build_plain(spec, s)
+    return s
+
+
+def test_staggered_requests_equal_alone():
+    srv = vg.ClothServer(hbm_budget_bytes=2 << 30, max_cloths=8, substeps=3, iterations=4)
+    plan = [(0, 20, 7), (0, 33, 12), (2, 9, 5), (3, 40, 9), (6, 16, 3)]  # (arrival tick, side, frames)
+    ids, specs = {}, {}
+    tick = 0
+    while tick < 60:
+        for t, side, frames in plan:
+            if t == tick:
+                spec = request(side, 0.5 + 0.01 * side)
+                s = registered(spec)
+                rid = srv.submit(s, frames)
+                s.close()  # the server keeps its own copy
+                ids[rid] = (side, frames)
+                specs[rid] = spec
+        info = srv.tick()
+        tick += 1
+        if tick > max(p[0] for p in plan) and info.active == 0 and info.queued == 0:
+            break
+    for rid, (side, frames) in ids.items():
+        st, done = srv.poll(rid)
+        assert st == _abi.REQ_DONE and done == frames
+        got = srv.result(rid)
+        want = alone(specs[rid], frames)
+        assert np.array_equal(bits(got), bits(want)), f"request side {side}"
+    stats = srv.stats()
+    assert stats.requests_done == len(plan)
+    assert stats.p99_frame_ms >= stats.p50_frame_ms > 0
+
+
+def test_admission_waits_for_budget_and_cap():
+    # a cap of 1000 active particles: the 32x32 request (1024) must wait until it runs alone
+    srv = vg.ClothServer(hbm_budget_bytes=1 << 30, max_cloths=4, max_active_particles=1000,
+                         substeps=2, iterations=2)
+    a = registered(request(20))   # 400 particles
+    b = registered(request(32))   # 1024 particles
+    ra = srv.submit(a, 3)
+    rb = srv.submit(b, 2)
+    info = srv.tick()
+    assert info.active == 1 and info.queued == 1
+    assert srv.poll(rb)[0] == _abi.REQ_QUEUED
+    for _ in range(3):
+        info = srv.tick()
+    assert srv.poll(ra)[0] == _abi.REQ_DONE and srv.poll(rb)[0] == _abi.REQ_ACTIVE
+    while srv.poll(rb)[0] != _abi.REQ_DONE:
+        srv.tick()
+    assert np.array_equal(bits(srv.result(rb)), bits(alone(request(32), 2, 2, 2)))
+
+
+def test_rejects_non_grid_and_oversize():
+    srv = vg.ClothServer(hbm_budget_bytes=1 << 27, max_cloths=2)  # ~310k particles of arena
+    s = vg.ClothSolver()
+    verts, idx = W.grid_mesh(3, 0.06)
+    s.add_cloth(verts, idx, np.eye(4), 0.03)
+    with pytest.raises(vg.VtError) as e:
+        srv.submit(s, 1)  # no grid constraint build: not a grid cloth
+    assert e.value.status == _abi.VT_ERR_INVALID_ARGUMENT
+    big = registered(request(700))  # 490k particles: more than a 128 MB arena holds
+    with pytest.raises(vg.VtError) as e:
+        srv.submit(big, 1)
+    assert e.value.status == _abi.VT_ERR_CAPACITY

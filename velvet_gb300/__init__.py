@@ -7,9 +7,9 @@ the benchmark use.  Nothing here computes physics on the CPU: if the library is 
 every call raises.
 """
 from ._abi import VtError, VtParams, VtSdfCollider, default_params, lib  # noqa: F401
-from .solver import BatchSolver, ClothSolver, colmajor, hash_objects, stream_handle  # noqa: F401
+from .solver import BatchSolver, ClothServer, ClothSolver, colmajor, hash_objects, stream_handle  # noqa: F401
 
 __all__ = [
-    "BatchSolver", "ClothSolver", "VtError", "VtParams", "VtSdfCollider", "default_params", "lib",
+    "BatchSolver", "ClothServer", "ClothSolver", "VtError", "VtParams", "VtSdfCollider", "default_params", "lib",
     "colmajor", "hash_objects", "stream_handle",
 ]

@@ -72,6 +72,41 @@ class VtStageTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
 
 
+class VtServerConfig(C.Structure):
+    """vt_server_config."""
+
+    _fields_ = [
+        ("hbm_budget_bytes", C.c_uint64),
+        ("max_cloths", C.c_uint32),
+        ("max_active_particles", C.c_uint32),
+        ("frame_dt", C.c_float),
+        ("substeps", C.c_int32),
+        ("iterations", C.c_int32),
+        ("relaxation", C.c_float),
+        ("friction", C.c_float),
+        ("collision_margin", C.c_float),
+    ]
+
+
+class VtServerTickInfo(C.Structure):
+    _fields_ = [
+        ("admitted", C.c_int32), ("retired", C.c_int32), ("active", C.c_int32), ("queued", C.c_int32),
+        ("active_particles", C.c_uint64), ("frame_ms", C.c_double),
+    ]
+
+
+class VtServerStats(C.Structure):
+    _fields_ = [
+        ("ticks", C.c_uint64), ("frames_done", C.c_uint64), ("requests_done", C.c_uint64),
+        ("particle_iterations", C.c_double), ("gpu_ms", C.c_double),
+        ("p50_frame_ms", C.c_double), ("p99_frame_ms", C.c_double),
+        ("bytes_in_use", C.c_uint64), ("bytes_budget", C.c_uint64),
+    ]
+
+
+REQ_QUEUED, REQ_ACTIVE, REQ_DONE = 0, 1, 2
+
+
 class VtHashParams(C.Structure):
     """vt_hash_params — HashParams (Velvet/SpatialHashGPU.cuh:7-15)."""
 
@@ -135,6 +170,13 @@ SIGNATURES: dict[str, tuple] = {
     "vt_batch_all_get": (I32, [P, I32, P, I32, P]),
     "vt_batch_launch_count": (I32, [P, C.POINTER(C.c_uint64)]),
     "vt_batch_use_graphs": (I32, [P, I32]),
+    "vt_server_create": (I32, [C.POINTER(VtServerConfig), C.POINTER(P)]),
+    "vt_server_destroy": (I32, [P]),
+    "vt_server_submit": (I32, [P, P, I32, C.POINTER(C.c_int64)]),
+    "vt_server_tick": (I32, [P, P, C.POINTER(VtServerTickInfo)]),
+    "vt_server_poll": (I32, [P, C.c_int64, PI32, PI32]),
+    "vt_server_result": (I32, [P, C.c_int64, P, U32]),
+    "vt_server_stats_get": (I32, [P, C.POINTER(VtServerStats)]),
     "vt_profiler_enable": (I32, [I32]),
     "vt_profiler_reset": (I32, []),
     "vt_profiler_read": (I32, [C.POINTER(VtStageTime), U32, PU32]),

@@ -162,6 +162,12 @@ vt_status pull_state(SolverImpl* s);
 
 ColliderDev collider_to_device(const vt_sdf_collider& c);
 
+// Per-frame fields of a domain's parameter block from its vt_params and frame arguments.
+void fill_frame_params(DomainParams& D, const vt_params& P, const FrameArgs& a);
+// Grid domains: per-generator stretch rest lengths (from the constraint list) and
+// per-particle LRA rest distances, one float4 per particle each.
+void grid_rests(const HostSolver& h, float4* grest, float4* glra);
+
 }  // namespace vt
 
 struct vt_solver : vt::SolverImpl {};

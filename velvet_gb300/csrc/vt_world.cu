@@ -411,31 +411,8 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
             D.grid_res = h.grid_res;
             D.grid_slot_begin = sb + h.grid_slot_begin;
             D.grid_slot_count = h.grid_slot_count;
-            const int32_t R = h.grid_res, V = R + 1;
-            // rest lengths per generator, read from the constraint list in its order
-            size_t c = 0;
-            for (int32_t X = 0; X <= R; ++X)
-                for (int32_t Y = 0; Y <= R; ++Y) {
-                    float r[4] = {0, 0, 0, 0};
-                    if (Y != R) r[0] = h.st_rest[c++];
-                    if (X != R) r[1] = h.st_rest[c++];
-                    if (X != R && Y != R) {
-                        r[2] = h.st_rest[c++];
-                        r[3] = h.st_rest[c++];
-                    }
-                    hgrest[pb + X * V + Y] = make_float4(r[0], r[1], r[2], r[3]);
-                }
-            // LRA rest distances |slot0 - x0_i| of the first slots
-            const int32_t ns = std::min(h.grid_slot_count, kGridLraCached);
-            for (int32_t i = 0; i < n; ++i) {
-                float r[4] = {0, 0, 0, 0};
-                const vec3 xi = mk3(h.x0[3 * i], h.x0[3 * i + 1], h.x0[3 * i + 2]);
-                for (int32_t s = 0; s < ns; ++s) {
-                    const float* q = &h.slots0[3 * (size_t)(h.grid_slot_begin + s)];
-                    r[s] = length(mk3(q[0], q[1], q[2]) - xi);
-                }
-                hglra[pb + i] = make_float4(r[0], r[1], r[2], r[3]);
-            }
+            const int32_t V = h.grid_res + 1;
+            grid_rests(h, hgrest.data() + pb, hglra.data() + pb);
             for (int32_t a = 0; a < V; a += kGridTA)
                 for (int32_t b = 0; b < V; b += kGridTB) gt.push_back(GridTile{k, a, b, 0});
             tiles_for(gpt, k, pb, n);
@@ -552,10 +529,37 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     return VT_OK;
 }
 
-void World::set_frame(int k, const HostSolver& h, const FrameArgs& a)
+void grid_rests(const HostSolver& h, float4* grest, float4* glra)
 {
-    DomainParams& D = hdom[k];
-    const vt_params& P = h.P;
+    const int32_t R = h.grid_res, V = R + 1, n = (int32_t)h.n();
+    size_t c = 0;  // rest lengths per generator, read from the constraint list in its order
+    for (int32_t X = 0; X <= R; ++X)
+        for (int32_t Y = 0; Y <= R; ++Y) {
+            float r[4] = {0, 0, 0, 0};
+            if (Y != R) r[0] = h.st_rest[c++];
+            if (X != R) r[1] = h.st_rest[c++];
+            if (X != R && Y != R) {
+                r[2] = h.st_rest[c++];
+                r[3] = h.st_rest[c++];
+            }
+            grest[X * V + Y] = make_float4(r[0], r[1], r[2], r[3]);
+        }
+    const int32_t ns = std::min(h.grid_slot_count, kGridLraCached);  // |slot0 - x0_i|
+    for (int32_t i = 0; i < n; ++i) {
+        float r[4] = {0, 0, 0, 0};
+        const vec3 xi = mk3(h.x0[3 * i], h.x0[3 * i + 1], h.x0[3 * i + 2]);
+        for (int32_t s = 0; s < ns; ++s) {
+            const float* q = &h.slots0[3 * (size_t)(h.grid_slot_begin + s)];
+            r[s] = length(mk3(q[0], q[1], q[2]) - xi);
+        }
+        glra[i] = make_float4(r[0], r[1], r[2], r[3]);
+    }
+}
+
+void World::set_frame(int k, const HostSolver& h, const FrameArgs& a) { fill_frame_params(hdom[k], h.P, a); }
+
+void fill_frame_params(DomainParams& D, const vt_params& P, const FrameArgs& a)
+{
     D.diameter = a.diameter;
     D.diameter2 = a.diameter * a.diameter;
     D.gx = P.gravity[0];

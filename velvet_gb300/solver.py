@@ -294,6 +294,60 @@ class BatchSolver:
         check(lib().vt_batch_use_graphs(self._h, 1 if on else 0), "vt_batch_use_graphs")
 
 
+class ClothServer:
+    """Continuous batching of cloth requests (vt_server_*): submit grid cloths with a
+    frame count, call tick() repeatedly; each tick retires, admits and advances every
+    active request by one frame."""
+
+    def __init__(self, hbm_budget_bytes: int, max_cloths: int = 1024, max_active_particles: int = 0,
+                 frame_dt: float = 1 / 60, substeps: int = 5, iterations: int = 10, relaxation: float = 1.0,
+                 friction: float = 0.1, collision_margin: float = 0.06):
+        cfg = _abi.VtServerConfig(int(hbm_budget_bytes), max_cloths, max_active_particles, frame_dt, substeps,
+                                  iterations, relaxation, friction, collision_margin)
+        self.cfg = cfg
+        self._h = C.c_void_p()
+        check(lib().vt_server_create(C.byref(cfg), C.byref(self._h)), "vt_server_create")
+        self.sizes: dict[int, int] = {}
+
+    def close(self) -> None:
+        if self._h:
+            lib().vt_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, cloth: ClothSolver, frames: int) -> int:
+        rid = C.c_int64()
+        check(lib().vt_server_submit(self._h, cloth.handle, frames, C.byref(rid)), "vt_server_submit")
+        self.sizes[rid.value] = cloth.num_particles
+        return rid.value
+
+    def tick(self, stream=None) -> _abi.VtServerTickInfo:
+        info = _abi.VtServerTickInfo()
+        check(lib().vt_server_tick(self._h, stream_handle(stream), C.byref(info)), "vt_server_tick")
+        return info
+
+    def poll(self, rid: int) -> tuple[int, int]:
+        st, done = C.c_int32(), C.c_int32()
+        check(lib().vt_server_poll(self._h, rid, C.byref(st), C.byref(done)), "vt_server_poll")
+        return st.value, done.value
+
+    def result(self, rid: int) -> np.ndarray:
+        n = self.sizes[rid]
+        out = np.empty((n, 3), np.float32)
+        check(lib().vt_server_result(self._h, rid, _ptr(out), n), "vt_server_result")
+        return out
+
+    def stats(self) -> _abi.VtServerStats:
+        s = _abi.VtServerStats()
+        check(lib().vt_server_stats_get(self._h, C.byref(s)), "vt_server_stats_get")
+        return s
+
+
 def hash_objects(positions_dev: int, original_dev: int, n: int, cell_spacing: float,
                  table_size: int, max_neighbors: int, particle_diameter: float,
                  out_hash: int, out_index: int, out_cell_start: int, out_cell_end: int,

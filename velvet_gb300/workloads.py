@@ -218,6 +218,29 @@ def batched(count: int = 512, frames: int = 300, seed: int = 0, lo: int = 16, hi
     return Workload(f"batched_{count}", cloths, 5, 10, frames, seed=seed)
 
 
+def partition_cloths(costs, world: int) -> list[list[int]]:
+    """Splits cloth indices over `world` GPUs, balancing the summed cost (particles x
+    substeps x iterations): longest-processing-time-first greedy, ties to the lower
+    rank.  Deterministic, so every rank computes the same partition without talking."""
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0] * world
+    parts: list[list[int]] = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        parts[r].append(i)
+        load[r] += costs[i]
+    return [sorted(p) for p in parts]
+
+
+def shard(wl: Workload, rank: int, world: int) -> Workload:
+    """The cloths of `wl` that rank `rank` of `world` simulates (strong scaling)."""
+    costs = [c.num_particles * wl.substeps * wl.iterations for c in wl.cloths]
+    mine = partition_cloths(costs, world)[rank]
+    return Workload(f"{wl.name}_shard{rank}of{world}", [wl.cloths[i] for i in mine], wl.substeps,
+                    wl.iterations, wl.frames, wl.relaxation, wl.friction, wl.collision_margin,
+                    wl.frame_dt, wl.seed, dict(wl.notes, shard=(rank, world)))
+
+
 def build_plain(spec: ClothSpec, solver, params_scalar: float = 1.5) -> int:
     """Registers one cloth the way VtClothObjectGPU::Start does (AddCloth, then
     GenerateStretch / GenerateAttach / GenerateBending); returns the offset."""
