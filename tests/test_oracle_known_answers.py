@@ -44,6 +44,26 @@ def test_hash_coords_known_answers():
         assert L.vo_hash_coords(x, y, z, t) == py_hash(x, y, z, t), (x, y, z, t)
 
 
+def test_direct_remainder_identity_used_by_the_neighbour_kernel():
+    """The neighbour-cache kernel computes abs(h % T) as |h| mod T via
+    mulhi64((M * |h|) mod 2^64, T) with M = floor((2^64 - 1) / T) + 1 (Lemire, Kaser,
+    Kurz 2019); exact for all 32-bit operands."""
+    rng = np.random.default_rng(9)
+    ds = list(rng.integers(1, 2 ** 31 - 1, 3000)) + [1, 2, 3, 7, 8192, 131072, 2097152, 2 ** 31 - 1]
+    for d in ds:
+        d = int(d)
+        M = ((2 ** 64 - 1) // d + 1) % 2 ** 64
+        for h in list(rng.integers(-(2 ** 31), 2 ** 31 - 1, 20)) + [-(2 ** 31), -1, 0, 1, 2 ** 31 - 1]:
+            h = int(h)
+            n = (-h) % 2 ** 32 if h < 0 else h  # |h| as an unsigned 32-bit value
+            assert ((M * n) % 2 ** 64 * d) >> 64 == py_hash_mod(h, d)
+
+
+def py_hash_mod(h, table):
+    r = abs(h) % table
+    return r
+
+
 def test_int_coord_uses_fp32_division_and_floor():
     L = oracle.lib()
     rng = np.random.default_rng(2)

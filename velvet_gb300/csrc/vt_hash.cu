@@ -38,6 +38,18 @@ __device__ __forceinline__ uint32_t hash_coords(int32_t x, int32_t y, int32_t z,
     return (uint32_t)(r < 0 ? -r : r);
 }
 
+// abs(h % T) for the int32 h whose bits are `h`, via |h| mod T (C's remainder truncates
+// toward zero, so |h % T| = |h| mod T), with the remainder computed directly from a
+// precomputed 64-bit reciprocal M = floor((2^64 - 1) / T) + 1: n mod T =
+// mulhi64((M * n) mod 2^64, T), exact for every 32-bit n and T (Lemire, Kaser, Kurz,
+// "Faster remainder by direct computation", 2019).
+__device__ __forceinline__ uint32_t abs_mod(uint32_t h, uint64_t M, uint32_t T)
+{
+    const uint32_t n = ((int32_t)h < 0) ? 0u - h : h;
+    const uint64_t low = M * (uint64_t)n;
+    return (uint32_t)__umul64hi(low, (uint64_t)T);
+}
+
 // ------------------------------------------------------------------ keys
 __global__ void __launch_bounds__(kBlock)
 k_hash_keys(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
@@ -265,19 +277,29 @@ __device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* 
                                                     const uint32_t* __restrict__ ce, Pos pos, Pos orig,
                                                     uint32_t* __restrict__ out_base, uint32_t id_base,
                                                     int32_t n, int32_t table_base, int32_t table,
-                                                    float sp, float sp2, float diam2, int32_t max_nbr)
+                                                    uint64_t M, float sp, float sp2, float diam2,
+                                                    int32_t max_nbr)
 {
     const uint32_t id = vals[t];
     const vec3 position = pos(id);
-    const vec3 originalp = orig(id);
     const int32_t ix = int_coord(position.x, sp), iy = int_coord(position.y, sp),
                   iz = int_coord(position.z, sp);
     uint32_t* out = out_base + (id - id_base);
+    // the 27 keys are XORs of per-axis products: (x+dx)*A etc. wrap like x*A
+    uint32_t hx[3], hy[3], hz[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        hx[k] = (uint32_t)(ix - 1 + k) * 92837111u;
+        hy[k] = (uint32_t)(iy - 1 + k) * 689287499u;
+        hz[k] = (uint32_t)(iz - 1 + k) * 283923481u;
+    }
+    bool have_orig = false;
+    vec3 originalp = mk3(0, 0, 0);
     int cnt = 0;
-    for (int32_t x = ix - 1; x <= ix + 1; ++x)
-        for (int32_t y = iy - 1; y <= iy + 1; ++y)
-            for (int32_t z = iz - 1; z <= iz + 1; ++z) {
-                const uint32_t h = (uint32_t)table_base + hash_coords(x, y, z, table);
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            for (int c = 0; c < 3; ++c) {
+                const uint32_t h = (uint32_t)table_base + abs_mod(hx[a] ^ hy[b] ^ hz[c], M, (uint32_t)table);
                 const uint32_t start = cs[h];
                 if (start == 0xffffffffu) continue;
                 uint32_t end = ce[h];
@@ -285,9 +307,15 @@ __device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* 
                 if (lim < end) end = lim;
                 for (uint32_t k = start; k < end; ++k) {
                     const uint32_t nb = vals[k];
+                    if (nb == id) continue;
                     const vec3 d1 = position - pos(nb);
+                    if (!(dot(d1, d1) < sp2)) continue;
+                    if (!have_orig) {
+                        originalp = orig(id);
+                        have_orig = true;
+                    }
                     const vec3 d2 = originalp - orig(nb);
-                    if (nb != id && dot(d1, d1) < sp2 && dot(d2, d2) > diam2) {
+                    if (dot(d2, d2) > diam2) {
                         out[(size_t)cnt * n] = nb;
                         ++cnt;
                         if (cnt >= max_nbr) return;
@@ -321,18 +349,19 @@ k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict
     const DomainParams& D = doms[tl.dom];
     cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF4{p}, PosF4{x0}, nbr + D.nbr_base,
                         (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
-                        D.cell_spacing, D.cell_spacing2, D.diameter2, D.max_nbr);
+                        ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2,
+                        D.diameter2, D.max_nbr);
 }
 
 __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors_f3(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ cs,
                      const uint32_t* __restrict__ ce, const float* __restrict__ pos,
                      const float* __restrict__ orig, uint32_t* __restrict__ nbr, int32_t n,
-                     int32_t table, float sp, float sp2, float diam2, int32_t max_nbr)
+                     int32_t table, uint64_t M, float sp, float sp2, float diam2, int32_t max_nbr)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
     if (t >= n) return;
-    cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF3{pos}, PosF3{orig}, nbr, 0u, n, 0, table,
+    cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF3{pos}, PosF3{orig}, nbr, 0u, n, 0, table, M,
                         sp, sp2, diam2, max_nbr);
 }
 
@@ -388,7 +417,8 @@ k_cache_neighbors_arena(const int32_t* __restrict__ pdom, const DomainParams* __
     const DomainParams& D = doms[pdom[vals[t]]];
     cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF4{p}, PosF4{x0}, nbr + D.nbr_base,
                         (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
-                        D.cell_spacing, D.cell_spacing2, D.diameter2, D.max_nbr);
+                        ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2,
+                        D.diameter2, D.max_nbr);
 }
 
 cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pin, int32_t hw,
@@ -446,8 +476,9 @@ cudaError_t hash_objects_f3(uint32_t* phash, uint32_t* pindex, uint32_t* cell_st
     e = radix_sort_pairs(phash, pindex, keys_tmp, vals_tmp, hist, digit_tot, n, bits, st);
     if (e != cudaSuccess) return e;
     k_cell_ranges<<<blocks, kBlock, 0, st>>>(phash, n, cell_start, cell_end);
+    const uint64_t magic = ~0ull / (uint64_t)hp.table_size + 1ull;
     k_cache_neighbors_f3<<<blocks, kBlock, 0, st>>>(pindex, cell_start, cell_end, positions, original,
-                                                    neighbors, n, hp.table_size, hp.cell_spacing,
+                                                    neighbors, n, hp.table_size, magic, hp.cell_spacing,
                                                     hp.cell_spacing2, hp.particle_diameter2,
                                                     (int32_t)hp.max_num_neighbors);
     return cudaGetLastError();

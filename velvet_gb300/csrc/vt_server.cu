@@ -204,6 +204,7 @@ vt_status place(vt_server* s, Request* r, cudaStream_t st)
     D.max_nbr = h.P.max_num_neighbors;
     D.cell_spacing = h.cell_spacing;
     D.cell_spacing2 = h.cell_spacing * h.cell_spacing;
+    vt::set_table_magic(D);
     D.grid_res = h.grid_res;
     D.grid_slot_begin = sid * kSlotsPerCloth;
     D.grid_slot_count = h.grid_slot_count;

@@ -406,6 +406,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         D.max_nbr = h.P.max_num_neighbors;
         D.cell_spacing = h.cell_spacing;
         D.cell_spacing2 = h.cell_spacing * h.cell_spacing;
+        set_table_magic(D);
         tiles_for(pt, k, pb, n);
         if (g) {
             D.grid_res = h.grid_res;

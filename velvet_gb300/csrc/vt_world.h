@@ -45,8 +45,16 @@ struct DomainParams {
     int32_t grid_res;        // >= 1: one grid cloth of (grid_res+1)^2 particles, implicit topology
     int32_t grid_slot_begin, grid_slot_count;  // its LRA slots (global slot indices)
     float xpbd_bend;         // bend_compliance / dt_sub / dt_sub, evaluated in that order
-    int32_t pad_[2];
+    uint32_t tmod_lo, tmod_hi;  // floor((2^64 - 1) / table_size) + 1, for the cell-key remainder
 };
+
+// The 64-bit reciprocal of a hash table size used by the direct-remainder modulo.
+inline void set_table_magic(DomainParams& D)
+{
+    const uint64_t M = ~0ull / (uint64_t)(D.table_size > 0 ? D.table_size : 1) + 1ull;
+    D.tmod_lo = (uint32_t)M;
+    D.tmod_hi = (uint32_t)(M >> 32);
+}
 
 // Most LRA slots per grid cloth whose rest distances are precomputed per particle.
 constexpr int kGridLraCached = 4;
