@@ -91,6 +91,13 @@ def iteration_bytes(wl) -> float:
     return b
 
 
+# DRAM traffic of one k_grid_iter launch per particle: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum = 50.45 + 1.57 MB on a 1024x1024 cloth (1,050,625 particles,
+# two LRA slots); the kernel reads the same four float4 streams for every grid cloth, so
+# the figure scales with the particles a launch covers.
+GRID_ITER_DRAM_BYTES_PER_PARTICLE = (50.45e6 + 1.57e6) / 1050625
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
 
@@ -573,9 +580,14 @@ def main() -> None:
     t_iter_ms = (solve[1] + bend[1] + grid_it[1]) / iters if (solve[0] or grid_it[0]) else 0.0
     if t_iter_ms > 0:
         ach = iteration_bytes(wl) / (t_iter_ms / 1000.0) / 1e9
-        kern = "k_grid_iter" if grid_it[0] and not solve[0] else "k_bend + k_solve"
+        grid_only = grid_it[0] and not solve[0]
+        kern = "k_grid_iter" if grid_only else "k_bend + k_solve"
+        traffic = GRID_ITER_DRAM_BYTES_PER_PARTICLE * n_tot if grid_only else None
         roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                    "traffic": None, "kernel": f"{kern}: one Jacobi iteration over all cloths",
+                    "traffic": traffic,
+                    "traffic_source": ("ncu DRAM bytes of k_grid_iter on a 1024x1024 cloth, scaled by particles"
+                                       if traffic else None),
+                    "kernel": f"{kern}: one Jacobi iteration over all cloths",
                     "algorithmic_bytes_per_launch": iteration_bytes(wl),
                     "avg_iteration_ms": t_iter_ms, "peak_source": f"{peak_kind} hbm_gbs",
                     "stage_ms_per_frame": {k: round(v[1] / 2, 4) for k, v in prof.items()}}
@@ -604,6 +616,7 @@ def main() -> None:
     ncol = sum(len(c.colliders(0)) for c in wl.cloths)
     h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
     d2h = n_tot * 24
+    grid_tile = ["7x31", "15x15", "3x63"][batch.grid_tile()] if batch.grid_tile() >= 0 else None
     batch.close()
 
     # ---- the plain drop-in solver on the same workload, one cloth at a time
@@ -633,7 +646,7 @@ def main() -> None:
             "data": "synthetic grid cloths generated from the config (seeded), no dataset",
             "config": {"workload": wl.name, "form": "batched (one graph launch per frame for all cloths)",
                        "cloths_per_gpu": len(wl.cloths), "particles_per_gpu": n_tot,
-                       "substeps": wl.substeps, "iterations": wl.iterations,
+                       "substeps": wl.substeps, "iterations": wl.iterations, "grid_tile": grid_tile,
                        "l2": "inputs larger than L2 (working set ~%.1f GB)" % (n_tot * 500 / 1e9),
                        "parallelism": f"independent cloths per GPU x {world} GPU(s)"},
             "p50_frame_ms": statistics.median(per), "p99_frame_ms": pct(per, 0.99),

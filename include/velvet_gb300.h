@@ -355,6 +355,17 @@ vt_status vt_server_result(vt_server* s, int64_t request_id, float* dst, uint32_
 
 vt_status vt_server_stats_get(vt_server* s, vt_server_stats* out);
 
+/* ------------------------------------------------------------------ tuning
+ * The grid-cloth kernel has several tile shapes; on its first frame a solver, batch or
+ * server times them on its own cloths and keeps the fastest (decisions are cached per
+ * size signature for the process).  The shape never changes a result.  This forces one
+ * shape for all handles created or tuned afterwards: 0 = 7x31, 1 = 15x15, 2 = 3x63;
+ * -1 returns to autotuning. */
+vt_status vt_tuning_set_grid_tile(int32_t variant);
+/* The shape in use by a solver / batch (after its first frame). */
+vt_status vt_solver_grid_tile(const vt_solver* s, int32_t* variant);
+vt_status vt_batch_grid_tile(const vt_batch* b, int32_t* variant);
+
 /* ------------------------------------------------------------------ profiler
  * Per-stage GPU timing, the counterpart of the reference's ScopedTimerGPU labels
  * (Velvet/Timer.hpp:95-151, 242-260): while enabled, every stage launch of every

@@ -79,9 +79,12 @@ def test_batch_launch_count_is_per_frame_not_per_cloth():
         s = vg.ClothSolver()
         W.build_plain(spec, s)
         batch.add(s)
-    batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin)
-    n1 = batch.launch_count()
-    batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin)
+    counts = []
+    for _ in range(3):
+        batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin)
+        counts.append(batch.launch_count())
     batch.sync()
-    per_frame = batch.launch_count() - n1
-    assert per_frame == n1 and per_frame < 40 + 3 * wl.substeps * wl.iterations
+    per_frame = counts[2] - counts[1]
+    # the first frame also times the grid tile shapes (a few extra launches, once)
+    assert per_frame == counts[1] - counts[0] and counts[0] >= per_frame
+    assert per_frame < 40 + 3 * wl.substeps * wl.iterations

@@ -92,6 +92,25 @@ def test_grid_tiles_at_every_edge_case(tile_edge):
     same(g.velocities(), o.velocities(), f"side {tile_edge} velocities")
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_every_grid_tile_shape_gives_the_same_bits(variant):
+    """The autotuner chooses among tile shapes; each must reproduce the oracle exactly."""
+    import ctypes as C
+
+    assert vg.lib().vt_tuning_set_grid_tile(variant) == 0
+    try:
+        spec = spec_of(37, 0.4)  # 37 leaves partial tiles for every shape
+        o, g = Oracle(), vg.ClothSolver()
+        for s in (o, g):
+            W.build_plain(spec, s)
+        run_frames([o, g], spec, 4)
+        same(g.positions(), o.positions(), f"tile shape {variant}")
+        used = C.c_int32()
+        assert vg.lib().vt_solver_grid_tile(g.handle, C.byref(used)) == 0 and used.value == variant
+    finally:
+        vg.lib().vt_tuning_set_grid_tile(-1)
+
+
 @pytest.mark.parametrize("case", ["no_self_collision", "zero_iterations", "hash_every_substep",
                                   "bend_compliance", "no_friction", "relaxation", "max_neighbors_8"])
 def test_schedule_branches(case):

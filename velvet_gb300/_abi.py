@@ -177,6 +177,9 @@ SIGNATURES: dict[str, tuple] = {
     "vt_server_poll": (I32, [P, C.c_int64, PI32, PI32]),
     "vt_server_result": (I32, [P, C.c_int64, P, U32]),
     "vt_server_stats_get": (I32, [P, C.POINTER(VtServerStats)]),
+    "vt_tuning_set_grid_tile": (I32, [I32]),
+    "vt_solver_grid_tile": (I32, [P, PI32]),
+    "vt_batch_grid_tile": (I32, [P, PI32]),
     "vt_profiler_enable": (I32, [I32]),
     "vt_profiler_reset": (I32, []),
     "vt_profiler_read": (I32, [C.POINTER(VtStageTime), U32, PU32]),

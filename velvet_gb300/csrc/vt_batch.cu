@@ -259,6 +259,13 @@ vt_status vt_batch_launch_count(const vt_batch* b, uint64_t* out)
     return VT_OK;
 }
 
+vt_status vt_batch_grid_tile(const vt_batch* b, int32_t* variant)
+{
+    VT_CHECK(b && variant, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *variant = b->world.grid_variant;
+    return VT_OK;
+}
+
 vt_status vt_batch_use_graphs(vt_batch* b, int32_t on)
 {
     VT_CHECK(b, VT_ERR_INVALID_ARGUMENT, "NULL batch");

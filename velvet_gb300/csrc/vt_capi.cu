@@ -683,6 +683,15 @@ vt_status vt_solver_use_graphs(vt_solver* s, int32_t on)
     return VT_OK;
 }
 
+vt_status vt_tuning_set_grid_tile(int32_t variant) { return vt::tuning_force(variant); }
+
+vt_status vt_solver_grid_tile(const vt_solver* s, int32_t* variant)
+{
+    VT_CHECK(s && variant, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *variant = s->world.grid_variant;
+    return VT_OK;
+}
+
 vt_status vt_profiler_enable(int32_t on) { return vt::profiler_enable(on != 0); }
 vt_status vt_profiler_reset(void) { return vt::profiler_reset(); }
 vt_status vt_profiler_read(vt_stage_time* out, uint32_t capacity, uint32_t* count)

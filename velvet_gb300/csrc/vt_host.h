@@ -127,6 +127,12 @@ public:
     int32_t n_domains = 0, n_particles = 0, n_bends = 0, n_slots = 0, n_cols = 0;
     int32_t total_keys = 0, n_ptiles = 0, n_btiles = 0, nbr_words = 0;
     int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
+    int32_t grid_variant = 0;  // tile shape of the grid kernel (kGridShape index)
+    // Times every grid tile shape on this world's cloths (one Jacobi iteration each, from
+    // the current positions, into scratch buffers) and keeps the fastest; decisions are
+    // cached per size signature for the process.  Never changes a result.
+    vt_status autotune(cudaStream_t st);
+    vt_status set_grid_variant(int variant);
     int32_t pcur = 0;  // which of p[0], p[1] holds the latest predicted positions
     uint64_t bytes = 0;
     uint64_t launches = 0;  // kernels enqueued so far
@@ -138,6 +144,9 @@ private:
     size_t staging_bytes_ = 0;
     cudaEvent_t staged_ = nullptr;
     bool cols_dirty_ = true, slots_dirty_ = true;
+    bool tuned_ = false;
+    std::vector<std::pair<int32_t, int32_t>> grid_doms_;  // (domain, resolution) of grid domains
+    int32_t gtiles_cap_ = 0;
     // frame graph
     cudaStream_t cap_ = nullptr;
     cudaGraphExec_t gexec_ = nullptr;
@@ -161,6 +170,13 @@ struct SolverImpl {
 vt_status pull_state(SolverImpl* s);
 
 ColliderDev collider_to_device(const vt_sdf_collider& c);
+
+// Grid tile shape to use: the forced one (vt_tuning_set), else `tuned`.
+int grid_variant_for(int tuned);
+// Last autotuned shape in this process (0 if none), for worlds that do not tune.
+int last_tuned_variant();
+// Forces a grid tile shape for every world (-1: autotune again).
+vt_status tuning_force(int32_t variant);
 
 // Per-frame fields of a domain's parameter block from its vt_params and frame arguments.
 void fill_frame_params(DomainParams& D, const vt_params& P, const FrameArgs& a);

@@ -24,6 +24,24 @@ namespace vt {
 
 static constexpr int kBlock = 256;
 
+// 16-byte asynchronous global -> shared copies (cp.async through L2); the zero-fill form
+// reads nothing and writes zeros when `valid` is false.  Both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16_zfill(void* smem, const void* gmem, bool valid)
+{
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // ------------------------------------------------------------------ colliders
 __device__ __forceinline__ float sgnf(float v) { return (v > 0) ? 1.0f : (v < 0 ? -1.0f : 0.0f); }
 
@@ -269,12 +287,13 @@ __device__ __forceinline__ void attach_one(vec3 pi, float wi, vec3 slot, float t
 }
 
 // ApplyDeltas (VtClothSolverGPU.cu:253-264) and, by mode, Finalize (:388-407) and the
-// next substep's PredictPositions (:42-53); writes x, v, p_out of particle i.
+// next substep's PredictPositions (:42-53); writes x, v, p_out of particle i.  `xsrc`
+// holds x[i] (global memory, or a shared-memory copy staged by the caller).
 template <int kMode>
 __device__ __forceinline__ void apply_and_finalize(const DomainParams& D, int dom, int i, vec3 pi, float wi,
-                                                   vec3 acc, int cnt, float4* __restrict__ pout,
-                                                   float4* __restrict__ x, float4* __restrict__ v,
-                                                   int32_t* __restrict__ status)
+                                                   vec3 acc, int cnt, const float4* xsrc,
+                                                   float4* __restrict__ pout, float4* __restrict__ x,
+                                                   float4* __restrict__ v, int32_t* __restrict__ status)
 {
     if (cnt > 0) {
         const float count = (float)cnt;
@@ -285,7 +304,7 @@ __device__ __forceinline__ void apply_and_finalize(const DomainParams& D, int do
         return;
     }
     const float dt = D.dt_sub;
-    const float4 x4 = x[i];
+    const float4 x4 = *xsrc;
     const vec3 xi = xyz(x4);
     vec3 np = pi;
     vec3 rv = (np - xi) / dt;
@@ -384,7 +403,7 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
             cnt++;
         }
     }
-    apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, pout, x, v, status);
+    apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, x + i, pout, x, v, status);
 }
 
 // ------------------------------------------------------------------ grid tile iteration
@@ -403,10 +422,7 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
 // particle's LRA rest distances (glra, up to kGridLraCached slots) are evaluated once
 // at registration with the same FP32 operations instead of every iteration: the kernel
 // is bound by instruction issue, HBM is mostly idle.
-constexpr int kGHA = kGridTA + 2, kGHB = kGridTB + 2;  // halo tile 9 x 33
-constexpr int kGGA = kGridTA + 1, kGGB = kGridTB + 1;  // generators 8 x 32
-
-template <int kMode>
+template <int kMode, int kTA, int kTB>
 __global__ void __launch_bounds__(kBlock, 4)
 k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__ doms,
             const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ x,
@@ -414,57 +430,83 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
             const float4* __restrict__ glra, const float4* __restrict__ slots,
             const float4* __restrict__ slots0, int32_t* __restrict__ status)
 {
+    constexpr int kGridTA = kTA, kGridTB = kTB;
+    constexpr int kGHA = kTA + 2, kGHB = kTB + 2;  // halo tile
+    constexpr int kGGA = kTA + 1, kGGB = kTB + 1;  // generators, kGGA * kGGB == kBlock
+    static_assert(kGGA * kGGB == kBlock, "one generator per thread");
     __shared__ float4 sp[kGHA][kGHB];
     __shared__ float4 sst[4][kGGA][kGGB];  // stretch common + fired flag, per type
     __shared__ float4 sbd[4][kGGA][kGGB];  // bending corner corrections + fired flag
+    __shared__ float4 sgr[kBlock];         // the generator's four stretch rest lengths
+    __shared__ float4 sgl[kBlock];         // the particle's LRA rest distances
+    __shared__ float4 sx[kBlock];          // the particle's position (finalizing modes)
+    __shared__ float4 sslot[kGridLraCached];
+    __shared__ __align__(16) DomainParams sdom;
+    static_assert(sizeof(DomainParams) % 16 == 0, "DomainParams is staged in 16-byte pieces");
     const GridTile tl = tiles[blockIdx.x];
-    const DomainParams& D = doms[tl.dom];
-    const int R = D.grid_res, V = R + 1, base = D.p_begin;
-    const int a0 = tl.a0, b0 = tl.b0;
     const int tid = (int)threadIdx.x;
+    const DomainParams& G = doms[tl.dom];
+    const int R = G.grid_res, V = R + 1, base = G.p_begin;
+    const int ns = G.grid_slot_count, s0 = G.grid_slot_begin;
+    const int a0 = tl.a0, b0 = tl.b0;
+    const int gx = tid / kGGB, gy = tid - gx * kGGB;  // this thread's generator
+    const int ta = tid / kGridTB, tb = tid - ta * kGridTB;  // this thread's particle
+    const int a = a0 + ta, b = b0 + tb;
+    const bool owns = tid < kGridTA * kGridTB && a < V && b < V;
+    const int i = base + a * V + b;
 
-    // 1. halo tile of predicted positions
+    // 1. stage with asynchronous copies (no registers held across the wait): the halo
+    // tile of predicted positions, each generator's rests, each particle's LRA rests and
+    // position, the LRA slots and the domain's parameters
     for (int k = tid; k < kGHA * kGHB; k += kBlock) {
         const int ha = k / kGHB, hb = k - ha * kGHB;
-        const int a = a0 - 1 + ha, b = b0 - 1 + hb;
-        float4 q = make_float4(0, 0, 0, 0);
-        if (a >= 0 && a < V && b >= 0 && b < V) q = pin[base + a * V + b];
-        sp[ha][hb] = q;
+        const int pa = a0 - 1 + ha, pb = b0 - 1 + hb;
+        const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V;
+        cp_async16_zfill(&sp[ha][hb], pin + (in ? base + pa * V + pb : base), in);
     }
-    __syncthreads();
-
-    // 2. generators (x, y) = (a0 - 1 + gx, b0 - 1 + gy): one per thread
     {
-        const int gx = tid / kGGB, gy = tid - gx * kGGB;
+        const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
+        const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
+        cp_async16_zfill(&sgr[tid], grest + (gen ? base + X * V + Y : base), gen);
+    }
+    if (owns && ns >= 1 && ns <= kGridLraCached) cp_async16(&sgl[tid], glra + i);
+    if (kMode != SOLVE_PLAIN && owns) cp_async16(&sx[tid], x + i);
+    if (tid < ns && tid < kGridLraCached) cp_async16(&sslot[tid], slots + s0 + tid);
+    if (tid < (int)(sizeof(DomainParams) / 16))
+        cp_async16(reinterpret_cast<float4*>(&sdom) + tid, reinterpret_cast<const float4*>(&G) + tid);
+    cp_async_wait_all();
+    __syncthreads();
+    const DomainParams& D = sdom;
+
+    // 2. generators (x, y) = (a0 - 1 + gx, b0 - 1 + gy): one per thread; each result goes
+    // to shared memory as soon as it is known
+    {
         const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
         const float4 zero = make_float4(0, 0, 0, 0);
-        float4 s0 = zero, s1 = zero, s2 = zero, s3 = zero;
+        const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
+        const bool full = gen && X < R && Y < R;
+        const float4 pxy = sp[gx][gy];
+        const float4 rest = sgr[tid];
+        vec3 cm;
+        float4 r = zero;
+        if (gen && Y < R && stretch_common(pxy, sp[gx][gy + 1], rest.x, cm))  // t0: (x,y)-(x,y+1)
+            r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+        sst[0][gx][gy] = r;
+        r = zero;
+        if (gen && X < R && stretch_common(pxy, sp[gx + 1][gy], rest.y, cm))  // t1: (x,y)-(x+1,y)
+            r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+        sst[1][gx][gy] = r;
+        r = zero;
+        if (full && stretch_common(pxy, sp[gx + 1][gy + 1], rest.z, cm))  // t2: (x,y)-(x+1,y+1)
+            r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+        sst[2][gx][gy] = r;
+        r = zero;
+        if (full && stretch_common(sp[gx][gy + 1], sp[gx + 1][gy], rest.w, cm))  // t3: (x,y+1)-(x+1,y)
+            r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+        sst[3][gx][gy] = r;
         float4 c0 = zero, c1 = zero, c2 = zero, c3 = zero;
-        if (X >= 0 && Y >= 0 && X <= R && Y <= R) {
-            const float4 pxy = sp[gx][gy];
-            const float4 rest = grest[base + X * V + Y];
-            vec3 cm;
-            if (Y < R) {  // t0: (x,y)-(x,y+1)
-                if (stretch_common(pxy, sp[gx][gy + 1], rest.x, cm)) s0 = make_float4(cm.x, cm.y, cm.z, 1.0f);
-            }
-            if (X < R) {  // t1: (x,y)-(x+1,y)
-                if (stretch_common(pxy, sp[gx + 1][gy], rest.y, cm)) s1 = make_float4(cm.x, cm.y, cm.z, 1.0f);
-            }
-            if (X < R && Y < R) {
-                // t2: (x,y)-(x+1,y+1)
-                if (stretch_common(pxy, sp[gx + 1][gy + 1], rest.z, cm)) s2 = make_float4(cm.x, cm.y, cm.z, 1.0f);
-                // t3: (x,y+1)-(x+1,y)
-                if (stretch_common(sp[gx][gy + 1], sp[gx + 1][gy], rest.w, cm))
-                    s3 = make_float4(cm.x, cm.y, cm.z, 1.0f);
-                // bend of quad (x, y): corners (x,y), (x+1,y+1), (x,y+1), (x+1,y)
-                bend_eval(pxy, sp[gx + 1][gy + 1], sp[gx][gy + 1], sp[gx + 1][gy], 0.0f, D.xpbd_bend,
-                          c0, c1, c2, c3);
-            }
-        }
-        sst[0][gx][gy] = s0;
-        sst[1][gx][gy] = s1;
-        sst[2][gx][gy] = s2;
-        sst[3][gx][gy] = s3;
+        if (full)  // bend of quad (x, y): corners (x,y), (x+1,y+1), (x,y+1), (x+1,y)
+            bend_eval(pxy, sp[gx + 1][gy + 1], sp[gx][gy + 1], sp[gx + 1][gy], 0.0f, D.xpbd_bend, c0, c1, c2, c3);
         sbd[0][gx][gy] = c0;
         sbd[1][gx][gy] = c1;
         sbd[2][gx][gy] = c2;
@@ -473,13 +515,9 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     __syncthreads();
 
     // 3. particles of the tile
-    if (tid >= kGridTA * kGridTB) return;
-    const int ta = tid / kGridTB, tb = tid - ta * kGridTB;
-    const int a = a0 + ta, b = b0 + tb;
-    if (a >= V || b >= V) return;
-    const int i = base + a * V + b;
-    const int gx = ta + 1, gy = tb + 1;  // this particle's generator (a, b) and halo slot
-    const float4 pi4 = sp[gx][gy];
+    if (!owns) return;
+    const int hx = ta + 1, hy = tb + 1;  // this particle's generator (a, b) and halo slot
+    const float4 pi4 = sp[hx][hy];
     const vec3 pi = xyz(pi4);
     const float wi = pi4.w, nw = -wi;
     vec3 acc = mk3(0, 0, 0);
@@ -493,24 +531,23 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
         }                                           \
     } while (0)
     // stretch, constraint order: generators (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
-    if (a >= 1 && b >= 1) VT_TAKE(sst[2][gx - 1][gy - 1], wi);  // t2, second endpoint
-    if (a >= 1) VT_TAKE(sst[1][gx - 1][gy], wi);                // t1, second endpoint
-    if (a >= 1 && b < R) VT_TAKE(sst[3][gx - 1][gy], wi);       // t3, second endpoint
-    if (b >= 1) VT_TAKE(sst[0][gx][gy - 1], wi);                // t0, second endpoint
-    if (b >= 1 && a < R) VT_TAKE(sst[3][gx][gy - 1], nw);       // t3, first endpoint
-    if (b < R) VT_TAKE(sst[0][gx][gy], nw);                     // t0, first endpoint
-    if (a < R) VT_TAKE(sst[1][gx][gy], nw);                     // t1, first endpoint
-    if (a < R && b < R) VT_TAKE(sst[2][gx][gy], nw);            // t2, first endpoint
+    if (a >= 1 && b >= 1) VT_TAKE(sst[2][hx - 1][hy - 1], wi);  // t2, second endpoint
+    if (a >= 1) VT_TAKE(sst[1][hx - 1][hy], wi);                // t1, second endpoint
+    if (a >= 1 && b < R) VT_TAKE(sst[3][hx - 1][hy], wi);       // t3, second endpoint
+    if (b >= 1) VT_TAKE(sst[0][hx][hy - 1], wi);                // t0, second endpoint
+    if (b >= 1 && a < R) VT_TAKE(sst[3][hx][hy - 1], nw);       // t3, first endpoint
+    if (b < R) VT_TAKE(sst[0][hx][hy], nw);                     // t0, first endpoint
+    if (a < R) VT_TAKE(sst[1][hx][hy], nw);                     // t1, first endpoint
+    if (a < R && b < R) VT_TAKE(sst[2][hx][hy], nw);            // t2, first endpoint
 #undef VT_TAKE
     // long-range attachments, slot order
-    if (D.grid_slot_count) {
-        const int s0 = D.grid_slot_begin, ns = D.grid_slot_count;
+    if (ns) {
         if (ns <= kGridLraCached) {
-            const float4 r4 = glra[i];
+            const float4 r4 = sgl[tid];
             const float rs[4] = {r4.x, r4.y, r4.z, r4.w};
 #pragma unroll
             for (int k = 0; k < kGridLraCached; ++k)
-                if (k < ns) attach_one(pi, wi, xyz(slots[s0 + k]), rs[k] * D.lrs, acc, cnt);
+                if (k < ns) attach_one(pi, wi, xyz(sslot[k]), rs[k] * D.lrs, acc, cnt);
         } else {
             const vec3 x0i = xyz(x0[i]);
             for (int s = s0; s < s0 + ns; ++s) {
@@ -528,12 +565,12 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
             cnt++;                        \
         }                                 \
     } while (0)
-    if (a >= 1 && b >= 1) VT_CORNER(sbd[1][gx - 1][gy - 1]);
-    if (a >= 1 && b < R) VT_CORNER(sbd[3][gx - 1][gy]);
-    if (a < R && b >= 1) VT_CORNER(sbd[2][gx][gy - 1]);
-    if (a < R && b < R) VT_CORNER(sbd[0][gx][gy]);
+    if (a >= 1 && b >= 1) VT_CORNER(sbd[1][hx - 1][hy - 1]);
+    if (a >= 1 && b < R) VT_CORNER(sbd[3][hx - 1][hy]);
+    if (a < R && b >= 1) VT_CORNER(sbd[2][hx][hy - 1]);
+    if (a < R && b < R) VT_CORNER(sbd[0][hx][hy]);
 #undef VT_CORNER
-    apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, pout, x, v, status);
+    apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, &sx[tid], pout, x, v, status);
 }
 
 template <int kPredict>
@@ -667,33 +704,54 @@ cudaError_t launch_solve(const Launch& L, int pin, int pout, int mode)
     return cudaGetLastError();
 }
 
+template <int kMode, int kTA, int kTB>
+static cudaError_t carveout()
+{
+    return cudaFuncSetAttribute(k_grid_iter<kMode, kTA, kTB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                cudaSharedmemCarveoutMaxShared);
+}
+
+template <int kTA, int kTB>
+static cudaError_t carveout_modes()
+{
+    cudaError_t e = carveout<SOLVE_PLAIN, kTA, kTB>();
+    if (e == cudaSuccess) e = carveout<SOLVE_FINALIZE, kTA, kTB>();
+    if (e == cudaSuccess) e = carveout<SOLVE_FINALIZE_PREDICT, kTA, kTB>();
+    return e;
+}
+
 cudaError_t prepare_kernels()
 {
     // most shared memory per SM for the tile kernel: more resident tiles per SM
-    cudaError_t e = cudaFuncSetAttribute(k_grid_iter<SOLVE_PLAIN>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                         cudaSharedmemCarveoutMaxShared);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_grid_iter<SOLVE_FINALIZE>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_grid_iter<SOLVE_FINALIZE_PREDICT>,
-                                 cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    cudaError_t e = carveout_modes<kGridShape[0].ta, kGridShape[0].tb>();
+    if (e == cudaSuccess) e = carveout_modes<kGridShape[1].ta, kGridShape[1].tb>();
+    if (e == cudaSuccess) e = carveout_modes<kGridShape[2].ta, kGridShape[2].tb>();
     return e;
+}
+
+template <int kTA, int kTB>
+static void grid_iter_shape(const Launch& L, int pin, int pout, int mode)
+{
+    const DeviceArrays& d = *L.d;
+#define VT_GRID_ARGS \
+    d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.grest, d.glra, d.slots, d.slots0, d.status
+    if (mode == SOLVE_PLAIN)
+        k_grid_iter<SOLVE_PLAIN, kTA, kTB><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+    else if (mode == SOLVE_FINALIZE)
+        k_grid_iter<SOLVE_FINALIZE, kTA, kTB><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+    else
+        k_grid_iter<SOLVE_FINALIZE_PREDICT, kTA, kTB><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+#undef VT_GRID_ARGS
 }
 
 cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int mode)
 {
     if (!L.n_gtiles) return cudaSuccess;
-    const DeviceArrays& d = *L.d;
-#define VT_GRID_ARGS \
-    d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.grest, d.glra, d.slots, d.slots0, d.status
-    if (mode == SOLVE_PLAIN)
-        k_grid_iter<SOLVE_PLAIN><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
-    else if (mode == SOLVE_FINALIZE)
-        k_grid_iter<SOLVE_FINALIZE><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
-    else
-        k_grid_iter<SOLVE_FINALIZE_PREDICT><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
-#undef VT_GRID_ARGS
+    switch (L.grid_variant) {
+    case 1: grid_iter_shape<kGridShape[1].ta, kGridShape[1].tb>(L, pin, pout, mode); break;
+    case 2: grid_iter_shape<kGridShape[2].ta, kGridShape[2].tb>(L, pin, pout, mode); break;
+    default: grid_iter_shape<kGridShape[0].ta, kGridShape[0].tb>(L, pin, pout, mode); break;
+    }
     return cudaGetLastError();
 }
 

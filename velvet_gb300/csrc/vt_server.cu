@@ -120,7 +120,7 @@ struct vt_server {
     std::vector<vt::DomainParams> hdom;
     std::vector<vt::ColliderDev> hcol;
     std::vector<float4> hslots, hslots0;
-    int32_t n_ptiles = 0, n_gtiles = 0;
+    int32_t n_ptiles = 0, n_gtiles = 0, grid_variant = 0;
     std::vector<std::pair<double, int32_t>> frame_log;  // (frame ms, active requests)
     vt_server_stats stats{};
     uint64_t launches = 0;
@@ -226,13 +226,13 @@ vt_status upload_tables(vt_server* s, cudaStream_t st)
 {
     std::vector<vt::Tile> pt, gpt;
     std::vector<vt::GridTile> gt;
+    s->grid_variant = vt::last_tuned_variant();
     for (int32_t sid = 0; sid < (int32_t)s->slot.size(); ++sid) {
         const Request* r = s->slot[sid];
         if (!r) continue;
-        const int32_t pb = (int32_t)r->pb, n = (int32_t)r->n, V = r->h.grid_res + 1;
+        const int32_t pb = (int32_t)r->pb, n = (int32_t)r->n;
         for (int32_t b = pb; b < pb + n; b += 256) pt.push_back(vt::Tile{sid, b, std::min(pb + n, b + 256), 0});
-        for (int32_t a = 0; a < V; a += vt::kGridTA)
-            for (int32_t b = 0; b < V; b += vt::kGridTB) gt.push_back(vt::GridTile{sid, a, b, 0});
+        vt::grid_tiles_for(gt, sid, r->h.grid_res, s->grid_variant);
     }
     gpt = pt;
     if ((int32_t)pt.size() > s->cap_ptiles || (int32_t)gt.size() > s->cap_gtiles) {
@@ -265,7 +265,7 @@ vt_status upload_tables(vt_server* s, cudaStream_t st)
 // One frame of every active request.
 vt_status run_frame(vt_server* s, cudaStream_t st)
 {
-    vt::Launch L{&s->d, s->n_ptiles, 0, 0, st, 0, s->n_gtiles, s->n_ptiles};
+    vt::Launch L{&s->d, s->n_ptiles, 0, 0, st, 0, s->n_gtiles, s->n_ptiles, s->grid_variant};
     const vt_server_config& c = s->cfg;
     const int64_t hw = s->alloc.high_water();
     const uint32_t sentinel = (uint32_t)(3 * hw);
@@ -336,7 +336,8 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     cap = std::min<int64_t>(cap, (int64_t)INT32_MAX / kMaxNbr - 1);
     // tile tables: sides up to sqrt(cap); generators per tile 217 particles
     const int64_t cap_pt = cap / 256 + M + 1;
-    const int64_t cap_gt = cap / (vt::kGridTA * vt::kGridTB) + (int64_t)(0.2 * std::sqrt((double)cap * M)) + 2 * M + 16;
+    // grid tiles of the shape with the most tiles (3 x 63: ~V^2/189 + V/3 per cloth)
+    const int64_t cap_gt = cap / 189 + (int64_t)(0.4 * std::sqrt((double)cap * M)) + 2 * M + 16;
     // the arena
     auto tiles_bytes = [&](int64_t nt, size_t sz) { return ((nt * sz + 255) & ~size_t(255)); };
     const size_t a16 = ((size_t)cap * 16 + 255) & ~size_t(255), a4 = ((size_t)cap * 4 + 255) & ~size_t(255);

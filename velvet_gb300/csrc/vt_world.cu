@@ -163,6 +163,37 @@ vt_status profiler_read(vt_stage_time* out, uint32_t cap, uint32_t* count)
     return VT_OK;
 }
 
+// ------------------------------------------------------------------ tuning state
+namespace {
+std::mutex g_tune_mu;
+int g_forced_variant = -1;
+int g_last_tuned = 0;
+std::vector<std::pair<std::vector<int64_t>, int>> g_tune_cache;  // signature -> shape
+}  // namespace
+
+int grid_variant_for(int tuned)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    return g_forced_variant >= 0 ? g_forced_variant : tuned;
+}
+
+int last_tuned_variant()
+{
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    return g_forced_variant >= 0 ? g_forced_variant : g_last_tuned;
+}
+
+vt_status tuning_force(int32_t variant)
+{
+    if (variant < -1 || variant >= kGridShapes) {
+        set_error("grid tile variant out of range");
+        return VT_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_forced_variant = variant;
+    return VT_OK;
+}
+
 ColliderDev collider_to_device(const vt_sdf_collider& c)
 {
     ColliderDev d{};
@@ -215,8 +246,86 @@ void World::release()
     hdom.clear();
     hcol.clear();
     hslots.clear();
+    grid_doms_.clear();
     built_ = false;
+    tuned_ = false;
     bytes = 0;
+}
+
+vt_status World::set_grid_variant(int variant)
+{
+    std::vector<GridTile> gt;
+    for (auto& gd : grid_doms_) grid_tiles_for(gt, gd.first, gd.second, variant);
+    if ((int32_t)gt.size() > gtiles_cap_) {
+        set_error("grid tile table capacity exceeded");
+        return VT_ERR_STATE;
+    }
+    if (!gt.empty())
+        VT_CUDA(cudaMemcpy(d.gtiles, gt.data(), gt.size() * sizeof(GridTile), cudaMemcpyHostToDevice),
+                "upload gtiles");
+    n_gtiles = (int32_t)gt.size();
+    grid_variant = variant;
+    if (gexec_) {  // a captured frame bakes in the tile count
+        cudaGraphExecDestroy(gexec_);
+        gexec_ = nullptr;
+        gkey_[0] = -1;
+    }
+    return VT_OK;
+}
+
+vt_status World::autotune(cudaStream_t st)
+{
+    tuned_ = true;
+    if (grid_doms_.empty()) return VT_OK;
+    int forced = -1;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        forced = g_forced_variant;
+    }
+    if (forced >= 0) return forced == grid_variant ? VT_OK : set_grid_variant(forced);
+    // signature: cloth count and total particles (log2 buckets), mean side
+    int64_t parts = 0;
+    for (auto& gd : grid_doms_) parts += (int64_t)(gd.second + 1) * (gd.second + 1);
+    auto lg = [](int64_t v) { int b = 0; while ((1ll << b) < v) ++b; return (int64_t)b; };
+    const std::vector<int64_t> sig{lg((int64_t)grid_doms_.size()), lg(parts),
+                                   lg(parts / (int64_t)grid_doms_.size())};
+    int best = -1;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        for (auto& e : g_tune_cache)
+            if (e.first == sig) best = e.second;
+    }
+    if (best < 0) {
+        // time one Jacobi iteration per shape from the current positions (x -> p[0] -> p[1])
+        VT_CUDA(cudaMemcpyAsync(d.p[0], d.x, 16 * (size_t)n_particles, cudaMemcpyDeviceToDevice, st), "tune copy");
+        cudaEvent_t e0, e1;
+        VT_CUDA(cudaEventCreate(&e0), "event");
+        VT_CUDA(cudaEventCreate(&e1), "event");
+        float best_ms = 0;
+        for (int v = 0; v < kGridShapes; ++v) {
+            vt_status r = set_grid_variant(v);
+            if (r != VT_OK) return r;
+            Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles, n_gptiles, grid_variant};
+            VT_CUDA(launch_grid_iter(L, 0, 1, SOLVE_PLAIN), "tune warm-up");
+            VT_CUDA(cudaEventRecord(e0, st), "event");
+            for (int k = 0; k < 3; ++k) VT_CUDA(launch_grid_iter(L, 0, 1, SOLVE_PLAIN), "tune");
+            VT_CUDA(cudaEventRecord(e1, st), "event");
+            VT_CUDA(cudaEventSynchronize(e1), "tune sync");
+            float ms = 0;
+            VT_CUDA(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            launches += 4;
+            if (best < 0 || ms < best_ms) {
+                best = v;
+                best_ms = ms;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache.push_back({sig, best});
+        g_last_tuned = best;
+    }
+    return best == grid_variant ? VT_OK : set_grid_variant(best);
 }
 
 namespace {
@@ -412,10 +521,8 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
             D.grid_res = h.grid_res;
             D.grid_slot_begin = sb + h.grid_slot_begin;
             D.grid_slot_count = h.grid_slot_count;
-            const int32_t V = h.grid_res + 1;
             grid_rests(h, hgrest.data() + pb, hglra.data() + pb);
-            for (int32_t a = 0; a < V; a += kGridTA)
-                for (int32_t b = 0; b < V; b += kGridTB) gt.push_back(GridTile{k, a, b, 0});
+            grid_doms_.push_back({k, h.grid_res});
             tiles_for(gpt, k, pb, n);
         } else {
             D.grid_res = 0;
@@ -431,6 +538,15 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         nwb += h.P.max_num_neighbors * n;
         cb += (int32_t)h.colliders.size();
     }
+    // grid tiles of the shape to start with; capacity for the largest shape
+    gtiles_cap_ = 0;
+    for (int v = 0; v < kGridShapes; ++v) {
+        std::vector<GridTile> tmp;
+        for (auto& gd : grid_doms_) grid_tiles_for(tmp, gd.first, gd.second, v);
+        gtiles_cap_ = std::max(gtiles_cap_, (int32_t)tmp.size());
+    }
+    grid_variant = grid_variant_for(0);
+    for (auto& gd : grid_doms_) grid_tiles_for(gt, gd.first, gd.second, grid_variant);
     n_ptiles = (int32_t)pt.size();
     n_btiles = (int32_t)bt.size();
     n_stiles = (int32_t)st_tiles.size();
@@ -455,7 +571,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_cs = A.take<uint32_t>(TK), o_ce = A.take<uint32_t>(TK), o_nb = A.take<uint32_t>(NW);
     const size_t o_dom = A.take<DomainParams>(n_domains), o_col = A.take<ColliderDev>(C);
     const size_t o_pt = A.take<Tile>(pt.size()), o_bt = A.take<Tile>(bt.size());
-    const size_t o_stt = A.take<Tile>(st_tiles.size()), o_gt = A.take<GridTile>(gt.size());
+    const size_t o_stt = A.take<Tile>(st_tiles.size()), o_gt = A.take<GridTile>(gtiles_cap_);
     const size_t o_gpt = A.take<Tile>(gpt.size());
     const bool any_grid = !gt.empty();
     const size_t o_grest = A.take<float4>(any_grid ? N : 0), o_glra = A.take<float4>(any_grid ? N : 0);
@@ -517,6 +633,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         VT_CUDA(up(d.glra, hglra.data(), N * 16), "upload glra");
     }
     VT_CUDA(prepare_kernels(), "kernel attributes");
+    tuned_ = false;
     VT_CUDA(cudaMemset(d.status, 0, (1 + n_domains) * 4), "memset status");
 
     staging_bytes_ = sizeof(DomainParams) * n_domains + sizeof(ColliderDev) * C + 16 * SL + 64;
@@ -623,6 +740,10 @@ vt_status World::simulate(const FrameArgs& a, int32_t ih, bool any_self, cudaStr
     if (n_particles == 0) return VT_OK;
     vt_status r = upload_frame(st);
     if (r != VT_OK) return r;
+    if (!tuned_) {
+        r = autotune(st);
+        if (r != VT_OK) return r;
+    }
     if (!use_graph || profiler_on()) return enqueue_frame(a, ih, any_self, st);
     const int32_t key[4] = {a.substeps, a.iterations, ih, any_self ? 1 : 0};
     if (!gexec_ || std::memcmp(key, gkey_, sizeof(key)) != 0) {
@@ -685,7 +806,7 @@ vt_status World::upload_frame(cudaStream_t st)
 
 vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cudaStream_t st)
 {
-    Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles, n_gptiles};
+    Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles, n_gptiles, grid_variant};
     int pc = 0;
     int bits = 0;
     while ((1ll << bits) < (int64_t)total_keys) ++bits;

@@ -25,6 +25,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "../../include/velvet_gb300.h"
@@ -46,7 +47,9 @@ struct DomainParams {
     int32_t grid_slot_begin, grid_slot_count;  // its LRA slots (global slot indices)
     float xpbd_bend;         // bend_compliance / dt_sub / dt_sub, evaluated in that order
     uint32_t tmod_lo, tmod_hi;  // floor((2^64 - 1) / table_size) + 1, for the cell-key remainder
+    int32_t pad_;               // 128 bytes: kernels stage the block in 16-byte copies
 };
+static_assert(sizeof(DomainParams) == 128, "DomainParams layout");
 
 // The 64-bit reciprocal of a hash table size used by the direct-remainder modulo.
 inline void set_table_magic(DomainParams& D)
@@ -64,7 +67,21 @@ constexpr int kGridLraCached = 4;
 struct GridTile {
     int32_t dom, a0, b0, pad_;
 };
-constexpr int kGridTA = 7, kGridTB = 31;  // generators (TA+1) x (TB+1) = 8 x 32 = 256
+// Tile shapes of the grid kernel; every shape has (TA+1) x (TB+1) = 256 generators, one
+// per thread.  The shape changes which block computes what, never a result.
+struct GridShape {
+    int ta, tb;
+};
+constexpr int kGridShapes = 3;
+constexpr GridShape kGridShape[kGridShapes] = {{7, 31}, {15, 15}, {3, 63}};
+constexpr int kGridTA = 7, kGridTB = 31;  // shape 0
+// Tiles of shape `variant` covering a (res+1)^2 grid cloth of domain `dom`.
+inline void grid_tiles_for(std::vector<GridTile>& out, int dom, int res, int variant)
+{
+    const int V = res + 1, ta = kGridShape[variant].ta, tb = kGridShape[variant].tb;
+    for (int a = 0; a < V; a += ta)
+        for (int b = 0; b < V; b += tb) out.push_back(GridTile{dom, a, b, 0});
+}
 
 // One collider on the device: the reference's SDFCollider with VelocityAt's matrix
 // product lastTransform * invCurTransform precomputed (same arithmetic, once per frame).
@@ -128,6 +145,7 @@ struct Launch {
     int32_t n_particles;
     cudaStream_t st;
     int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
+    int32_t grid_variant = 0;  // tile shape of the gtiles (kGridShape index)
 };
 
 // One Jacobi iteration of the grid domains (stretch + attach + bending + ApplyDeltas,

@@ -179,6 +179,12 @@ class ClothSolver:
         a = np.ascontiguousarray(xyz, dtype=np.float32).reshape(3)
         check(lib().vt_attach_slot_set(self._h, slot, _ptr(a)), "vt_attach_slot_set")
 
+    def grid_tile(self) -> int:
+        """Tile shape the grid kernel uses (-1 before the first simulate)."""
+        v = C.c_int32()
+        check(lib().vt_solver_grid_tile(self._h, C.byref(v)), "vt_solver_grid_tile")
+        return v.value
+
     # ------------------------------------------------------------------ hash views
     def table_size(self) -> int:
         out = np.zeros(1, dtype=np.int32)
@@ -292,6 +298,12 @@ class BatchSolver:
 
     def use_graphs(self, on: bool) -> None:
         check(lib().vt_batch_use_graphs(self._h, 1 if on else 0), "vt_batch_use_graphs")
+
+    def grid_tile(self) -> int:
+        """Tile shape the grid kernel uses (-1 before the first simulate)."""
+        v = C.c_int32()
+        check(lib().vt_batch_grid_tile(self._h, C.byref(v)), "vt_batch_grid_tile")
+        return v.value
 
 
 class ClothServer:
