@@ -445,9 +445,8 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     static_assert(sizeof(DomainParams) % 16 == 0, "DomainParams is staged in 16-byte pieces");
     const GridTile tl = tiles[blockIdx.x];
     const int tid = (int)threadIdx.x;
-    const DomainParams& G = doms[tl.dom];
-    const int R = G.grid_res, V = R + 1, base = G.p_begin;
-    const int ns = G.grid_slot_count, s0 = G.grid_slot_begin;
+    const int R = tl.res, V = R + 1, base = tl.p_begin;
+    const int ns = tl.slot_count, s0 = tl.slot_begin;
     const int a0 = tl.a0, b0 = tl.b0;
     const int gx = tid / kGGB, gy = tid - gx * kGGB;  // this thread's generator
     const int ta = tid / kGridTB, tb = tid - ta * kGridTB;  // this thread's particle
@@ -473,7 +472,7 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     if (kMode != SOLVE_PLAIN && owns) cp_async16(&sx[tid], x + i);
     if (tid < ns && tid < kGridLraCached) cp_async16(&sslot[tid], slots + s0 + tid);
     if (tid < (int)(sizeof(DomainParams) / 16))
-        cp_async16(reinterpret_cast<float4*>(&sdom) + tid, reinterpret_cast<const float4*>(&G) + tid);
+        cp_async16(reinterpret_cast<float4*>(&sdom) + tid, reinterpret_cast<const float4*>(doms + tl.dom) + tid);
     cp_async_wait_all();
     __syncthreads();
     const DomainParams& D = sdom;

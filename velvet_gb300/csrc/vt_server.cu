@@ -232,7 +232,7 @@ vt_status upload_tables(vt_server* s, cudaStream_t st)
         if (!r) continue;
         const int32_t pb = (int32_t)r->pb, n = (int32_t)r->n;
         for (int32_t b = pb; b < pb + n; b += 256) pt.push_back(vt::Tile{sid, b, std::min(pb + n, b + 256), 0});
-        vt::grid_tiles_for(gt, sid, r->h.grid_res, s->grid_variant);
+        vt::grid_tiles_for(gt, sid, s->hdom[sid], s->grid_variant);
     }
     gpt = pt;
     if ((int32_t)pt.size() > s->cap_ptiles || (int32_t)gt.size() > s->cap_gtiles) {
@@ -345,8 +345,9 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     const size_t cells = ((size_t)cap * 3 * 4 + 255) & ~size_t(255), nbr = (size_t)cap * kMaxNbr * 4;
     const size_t small = M * (sizeof(vt::DomainParams) + kCollidersPerCloth * sizeof(vt::ColliderDev) +
                               2 * 16 * kSlotsPerCloth) + 4 * (M + 1) + 4096 * 4;
-    const size_t total = 8 * a16 + 5 * a4 + hist + 2 * cells + nbr + small + tiles_bytes(cap_pt, 16) * 2 +
-                         tiles_bytes(cap_gt, 16) + 64 * 256;
+    const size_t total = 8 * a16 + 5 * a4 + hist + 2 * cells + nbr + small +
+                         tiles_bytes(cap_pt, sizeof(vt::Tile)) * 2 + tiles_bytes(cap_gt, sizeof(vt::GridTile)) +
+                         64 * 256;
     VT_TRY_CUDA(cudaMalloc(&s->arena, total), "cudaMalloc(server arena)");
     char* b = (char*)s->arena;
     auto take = [&](size_t bytes) { char* p = b; b += (bytes + 255) & ~size_t(255); return (void*)p; };
@@ -375,7 +376,8 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     VT_TRY_CUDA(cudaMemset(s->d.status, 0, 4 * (M + 1)), "init status");
     VT_TRY_CUDA(cudaMemset(s->d.nbr, 0xff, nbr), "init neighbours");
     s->staging_bytes = M * (sizeof(vt::DomainParams) + kCollidersPerCloth * sizeof(vt::ColliderDev) +
-                            2 * 16 * kSlotsPerCloth) + (cap_pt * 2 + cap_gt) * 16 + 16 * 256;
+                            2 * 16 * kSlotsPerCloth) +
+                      cap_pt * 2 * sizeof(vt::Tile) + cap_gt * sizeof(vt::GridTile) + 16 * 256;
     VT_TRY_CUDA(cudaMallocHost(&s->staging, s->staging_bytes), "cudaMallocHost(server staging)");
     VT_TRY_CUDA(cudaEventCreateWithFlags(&s->staged, cudaEventDisableTiming), "event");
     VT_TRY_CUDA(cudaEventCreate(&s->ev0), "event");

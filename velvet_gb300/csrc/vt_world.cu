@@ -255,7 +255,7 @@ void World::release()
 vt_status World::set_grid_variant(int variant)
 {
     std::vector<GridTile> gt;
-    for (auto& gd : grid_doms_) grid_tiles_for(gt, gd.first, gd.second, variant);
+    for (auto& gd : grid_doms_) grid_tiles_for(gt, gd.first, hdom[gd.first], variant);
     if ((int32_t)gt.size() > gtiles_cap_) {
         set_error("grid tile table capacity exceeded");
         return VT_ERR_STATE;
@@ -542,11 +542,11 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     gtiles_cap_ = 0;
     for (int v = 0; v < kGridShapes; ++v) {
         std::vector<GridTile> tmp;
-        for (auto& gd : grid_doms_) grid_tiles_for(tmp, gd.first, gd.second, v);
+        for (auto& gd : grid_doms_) grid_tiles_for(tmp, gd.first, hdom[gd.first], v);
         gtiles_cap_ = std::max(gtiles_cap_, (int32_t)tmp.size());
     }
     grid_variant = grid_variant_for(0);
-    for (auto& gd : grid_doms_) grid_tiles_for(gt, gd.first, gd.second, grid_variant);
+    for (auto& gd : grid_doms_) grid_tiles_for(gt, gd.first, hdom[gd.first], grid_variant);
     n_ptiles = (int32_t)pt.size();
     n_btiles = (int32_t)bt.size();
     n_stiles = (int32_t)st_tiles.size();

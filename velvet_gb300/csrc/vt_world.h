@@ -63,9 +63,12 @@ inline void set_table_magic(DomainParams& D)
 constexpr int kGridLraCached = 4;
 
 // Grid tile: a TA x TB block of one grid cloth's particles, rows a in [a0, a0+TA),
-// columns b in [b0, b0+TB) of VertexAt(a, b) = a * (res+1) + b.
+// columns b in [b0, b0+TB) of VertexAt(a, b) = p_begin + a * (res+1) + b.  The fields a
+// block needs to address its loads are copied from the domain so that they arrive with
+// the tile's own load.
 struct GridTile {
-    int32_t dom, a0, b0, pad_;
+    int32_t dom, a0, b0, res;
+    int32_t p_begin, slot_begin, slot_count, pad_;
 };
 // Tile shapes of the grid kernel; every shape has (TA+1) x (TB+1) = 256 generators, one
 // per thread.  The shape changes which block computes what, never a result.
@@ -75,12 +78,13 @@ struct GridShape {
 constexpr int kGridShapes = 3;
 constexpr GridShape kGridShape[kGridShapes] = {{7, 31}, {15, 15}, {3, 63}};
 constexpr int kGridTA = 7, kGridTB = 31;  // shape 0
-// Tiles of shape `variant` covering a (res+1)^2 grid cloth of domain `dom`.
-inline void grid_tiles_for(std::vector<GridTile>& out, int dom, int res, int variant)
+// Tiles of shape `variant` covering the (grid_res+1)^2 grid cloth of domain `dom`.
+inline void grid_tiles_for(std::vector<GridTile>& out, int dom, const DomainParams& D, int variant)
 {
-    const int V = res + 1, ta = kGridShape[variant].ta, tb = kGridShape[variant].tb;
+    const int V = D.grid_res + 1, ta = kGridShape[variant].ta, tb = kGridShape[variant].tb;
     for (int a = 0; a < V; a += ta)
-        for (int b = 0; b < V; b += tb) out.push_back(GridTile{dom, a, b, 0});
+        for (int b = 0; b < V; b += tb)
+            out.push_back(GridTile{dom, a, b, D.grid_res, D.p_begin, D.grid_slot_begin, D.grid_slot_count, 0});
 }
 
 // One collider on the device: the reference's SDFCollider with VelocityAt's matrix
