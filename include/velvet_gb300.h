@@ -327,7 +327,8 @@ typedef struct vt_server_config {
 typedef struct vt_server_tick_info {
     int32_t  admitted, retired, active, queued;
     uint64_t active_particles;
-    double   frame_ms;             /* GPU time of this tick's frame (CUDA events)           */
+    double   frame_ms;             /* GPU time of the frame completed in this tick (the
+                                      previous tick's frame; CUDA events), 0 if none      */
 } vt_server_tick_info;
 
 typedef struct vt_server_stats {
@@ -345,7 +346,12 @@ vt_status vt_server_destroy(vt_server* s);
  * VT_ERR_CAPACITY if the request could never be admitted (larger than the budget). */
 vt_status vt_server_submit(vt_server* s, vt_solver* cloth, int32_t frames, int64_t* request_id);
 
-/* Retire, admit, one frame for every active request; waits for the frame to finish. */
+/* Retire requests whose frames are all enqueued, admit queued ones, enqueue one frame
+ * for every active request, then wait for the PREVIOUS tick's frame: the host work of a
+ * tick overlaps the GPU work of the one before.  `active` counts admitted requests whose
+ * result is not yet available; a request reaches VT_REQ_DONE one or two ticks after its
+ * last frame was enqueued.  Use one stream per server (a change of stream synchronises
+ * the old one first). */
 vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info);
 
 vt_status vt_server_poll(vt_server* s, int64_t request_id, int32_t* state, int32_t* frames_done);

@@ -111,6 +111,20 @@ def test_every_grid_tile_shape_gives_the_same_bits(variant):
         vg.lib().vt_tuning_set_grid_tile(-1)
 
 
+@pytest.mark.parametrize("n_slots", [5, 24])
+def test_many_lra_slots_recompute_their_rests(n_slots):
+    """More attach slots than the per-particle cache holds (the stress configuration
+    attaches a whole row): the tile kernel recomputes |slot0 - x0| for each slot."""
+    side = 24
+    spec = spec_of(side, 0.4, attached=list(range(0, side, side // n_slots))[:n_slots])
+    o, g = Oracle(), vg.ClothSolver()
+    for s in (o, g):
+        W.build_plain(spec, s)
+    run_frames([o, g], spec, 5)
+    same(g.positions(), o.positions(), f"{n_slots} LRA slots")
+    same(g.velocities(), o.velocities(), f"{n_slots} LRA slots velocities")
+
+
 @pytest.mark.parametrize("case", ["no_self_collision", "zero_iterations", "hash_every_substep",
                                   "bend_compliance", "no_friction", "relaxation", "max_neighbors_8"])
 def test_schedule_branches(case):

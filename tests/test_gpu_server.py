@@ -75,16 +75,43 @@ def test_admission_waits_for_budget_and_cap():
     info = srv.tick()
     assert info.active == 1 and info.queued == 1
     assert srv.poll(rb)[0] == _abi.REQ_QUEUED
-    for _ in range(3):
-        info = srv.tick()
-    assert srv.poll(ra)[0] == _abi.REQ_DONE and srv.poll(rb)[0] == _abi.REQ_ACTIVE
-    while srv.poll(rb)[0] != _abi.REQ_DONE:
+    for _ in range(40):
         srv.tick()
+        (sa, da), (sb, db) = srv.poll(ra), srv.poll(rb)
+        assert db == 0 or da == 3, "the large request ran beside the small one"
+        if sa == _abi.REQ_DONE and sb == _abi.REQ_DONE:
+            break
+    assert srv.poll(ra) == (_abi.REQ_DONE, 3) and srv.poll(rb) == (_abi.REQ_DONE, 2)
     assert np.array_equal(bits(srv.result(rb)), bits(alone(request(32), 2, 2, 2)))
+    assert np.array_equal(bits(srv.result(ra)), bits(alone(request(20), 3, 2, 2)))
+
+
+def test_ticks_overlap_host_work_with_the_previous_frame():
+    """A tick returns with its own frame still queued (it waits only for the previous
+    one), so a result appears a tick or two after its last frame; ranges freed by
+    finishing requests are reused at once.  Every request still ends with its bits
+    when simulated alone."""
+    srv = vg.ClothServer(hbm_budget_bytes=1 << 30, max_cloths=16, substeps=2, iterations=3)
+    specs, ids = {}, []
+    for k, side in enumerate([12, 40, 17, 64, 23, 9, 31, 50]):
+        spec = request(side, 0.4 + 0.01 * k)
+        s = registered(spec)
+        rid = srv.submit(s, 2 + k % 3)
+        s.close()
+        specs[rid] = (spec, 2 + k % 3)
+        ids.append(rid)
+    for _ in range(60):
+        info = srv.tick()
+        if info.active == 0 and info.queued == 0:
+            break
+    for rid in ids:
+        spec, frames = specs[rid]
+        assert srv.poll(rid) == (_abi.REQ_DONE, frames)
+        assert np.array_equal(bits(srv.result(rid)), bits(alone(spec, frames, 2, 3)))
 
 
 def test_rejects_non_grid_and_oversize():
-    srv = vg.ClothServer(hbm_budget_bytes=1 << 27, max_cloths=2)  # ~310k particles of arena
+    srv = vg.ClothServer(hbm_budget_bytes=1 << 27, max_cloths=2)  # ~300k particles of arena
     s = vg.ClothSolver()
     verts, idx = W.grid_mesh(3, 0.06)
     s.add_cloth(verts, idx, np.eye(4), 0.03)

@@ -214,8 +214,10 @@ static vt_status batch_get(vt_batch* b, int32_t index, int which, float* dst, in
     if (!n) return VT_OK;
     const float4* src = which == 0 ? b->world.d.x : which == 1 ? b->world.d.nrm : b->world.d.v;
     cudaStream_t st = (cudaStream_t)stream;
-    VT_TRY_CUDA(cudaMemcpy2DAsync(dst, 12, src + o, 16, 12, n,
-                                  on_dev ? cudaMemcpyDefault : cudaMemcpyDeviceToHost, st),
+    float* pk = b->world.d.packed + 3 * o;
+    VT_TRY_CUDA(vt::launch_pack_xyz(src + o, pk, (int64_t)n, st), "pack");
+    b->world.launches += 1;
+    VT_TRY_CUDA(cudaMemcpyAsync(dst, pk, 12 * n, on_dev ? cudaMemcpyDefault : cudaMemcpyDeviceToHost, st),
                 "copy out");
     if (!on_dev) VT_TRY_CUDA(cudaStreamSynchronize(st), "sync");
     return VT_OK;
@@ -245,8 +247,10 @@ vt_status vt_batch_all_get(vt_batch* b, int32_t what, float* dst, int32_t on_dev
     if (!n) return VT_OK;
     const float4* src = what == 0 ? b->world.d.x : what == 1 ? b->world.d.nrm : b->world.d.v;
     cudaStream_t st = (cudaStream_t)stream;
-    VT_TRY_CUDA(cudaMemcpy2DAsync(dst, 12, src, 16, 12, n,
-                                  on_dev ? cudaMemcpyDefault : cudaMemcpyDeviceToHost, st),
+    VT_TRY_CUDA(vt::launch_pack_xyz(src, b->world.d.packed, (int64_t)n, st), "pack");
+    b->world.launches += 1;
+    VT_TRY_CUDA(cudaMemcpyAsync(dst, b->world.d.packed, 12 * n, on_dev ? cudaMemcpyDefault : cudaMemcpyDeviceToHost,
+                                st),
                 "copy out");
     if (!on_dev) VT_TRY_CUDA(cudaStreamSynchronize(st), "sync");
     return VT_OK;

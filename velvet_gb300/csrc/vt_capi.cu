@@ -523,8 +523,11 @@ static vt_status get3(vt_solver* s, const float4* dev, const std::vector<float>&
     if (!count) return VT_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (dev) {
-        VT_TRY_CUDA(cudaMemcpy2DAsync(dst, 12, dev + first, 16, 12, count,
-                                      on_dev ? cudaMemcpyDefault : cudaMemcpyDeviceToHost, st),
+        float* pk = s->world.d.packed + 3 * (size_t)first;
+        VT_TRY_CUDA(vt::launch_pack_xyz(dev + first, pk, (int64_t)count, st), "pack");
+        s->world.launches += 1;
+        VT_TRY_CUDA(cudaMemcpyAsync(dst, pk, 12 * (size_t)count, on_dev ? cudaMemcpyDefault : cudaMemcpyDeviceToHost,
+                                    st),
                     "copy out");
         if (!on_dev) VT_TRY_CUDA(cudaStreamSynchronize(st), "sync");
         return VT_OK;

@@ -269,6 +269,38 @@ cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_s
     return cudaGetLastError();
 }
 
+// Cell ranges, plus the predicted and initial positions copied into sorted-slot order
+// (ps[t] = (p[vals[t]].xyz, bits of vals[t]), x0s[t] = x0[vals[t]]), so that the
+// neighbour walk reads a bucket's candidates, index included, as contiguous float4 runs
+// instead of gathering them through vals.
+__global__ void __launch_bounds__(kBlock)
+k_cell_ranges_gather(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                     const float4* __restrict__ p, const float4* __restrict__ x0, int32_t n,
+                     uint32_t* __restrict__ cs, uint32_t* __restrict__ ce, float4* __restrict__ ps,
+                     float4* __restrict__ x0s)
+{
+    const int t = blockIdx.x * kBlock + (int)threadIdx.x;
+    if (t >= n) return;
+    const uint32_t h = keys[t];
+    if (t == 0 || keys[t - 1] != h) {
+        cs[h] = (uint32_t)t;
+        if (t > 0) ce[keys[t - 1]] = (uint32_t)t;
+    }
+    if (t == n - 1) ce[h] = (uint32_t)n;
+    const uint32_t id = vals[t];
+    const float4 q = p[id];
+    ps[t] = make_float4(q.x, q.y, q.z, __uint_as_float(id));
+    x0s[t] = x0[id];
+}
+
+cudaError_t launch_cell_ranges_gather(const DeviceArrays& d, int pin, int32_t n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_cell_ranges_gather<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(d.keys, d.vals, d.p[pin], d.x0, n,
+                                                                      d.cell_start, d.cell_end, d.ps, d.x0s);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ neighbour cache
 // CacheNeighbors_Kernel, SpatialHashGPU.cu:79-130, for sorted slot t.
 template <typename Pos>
@@ -325,6 +357,69 @@ __device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* 
     out[(size_t)cnt * n] = 0xffffffffu;
 }
 
+// The same walk over sorted-slot copies of the positions: candidate k is ps[k] (its
+// position, its index in w) and x0s[k], one 16-byte load each, contiguous within a
+// bucket; the thread's own object is slot t, so the threads of a warp share buckets.
+// Same arithmetic, order and caps.  (Measured alternatives: threads in object order, a
+// warp per object, a warp per cell group, and (start, end) pairs loaded three buckets
+// at a time all ran slower — the walk is bound by load latency, and sorted order with
+// the highest occupancy gives the most shared bucket reads.)
+__device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint32_t* __restrict__ cs,
+                                                       const uint32_t* __restrict__ ce,
+                                                       const float4* __restrict__ ps,
+                                                       const float4* __restrict__ x0s,
+                                                       uint32_t* __restrict__ out_base, uint32_t id_base,
+                                                       int32_t n, int32_t table_base, int32_t table,
+                                                       uint64_t M, float sp, float sp2, float diam2,
+                                                       int32_t max_nbr)
+{
+    const float4 own = ps[t];
+    const uint32_t id = __float_as_uint(own.w);
+    const vec3 position = xyz(own);
+    const int32_t ix = int_coord(position.x, sp), iy = int_coord(position.y, sp),
+                  iz = int_coord(position.z, sp);
+    uint32_t* out = out_base + (id - id_base);
+    // the 27 keys are XORs of per-axis products: (x+dx)*A etc. wrap like x*A
+    uint32_t hx[3], hy[3], hz[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        hx[k] = (uint32_t)(ix - 1 + k) * 92837111u;
+        hy[k] = (uint32_t)(iy - 1 + k) * 689287499u;
+        hz[k] = (uint32_t)(iz - 1 + k) * 283923481u;
+    }
+    bool have_orig = false;
+    vec3 originalp = mk3(0, 0, 0);
+    int cnt = 0;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            for (int c = 0; c < 3; ++c) {
+                const uint32_t h = (uint32_t)table_base + abs_mod(hx[a] ^ hy[b] ^ hz[c], M, (uint32_t)table);
+                const uint32_t start = cs[h];
+                if (start == 0xffffffffu) continue;
+                uint32_t end = ce[h];
+                const uint32_t lim = start + (uint32_t)max_nbr;
+                if (lim < end) end = lim;
+                for (uint32_t k = start; k < end; ++k) {
+                    const float4 qk = ps[k];
+                    const uint32_t nb = __float_as_uint(qk.w);
+                    const vec3 d1 = position - xyz(qk);
+                    if (nb == id) continue;
+                    if (!(dot(d1, d1) < sp2)) continue;
+                    if (!have_orig) {
+                        originalp = xyz(x0s[t]);
+                        have_orig = true;
+                    }
+                    const vec3 d2 = originalp - xyz(x0s[k]);
+                    if (dot(d2, d2) > diam2) {
+                        out[(size_t)cnt * n] = nb;
+                        ++cnt;
+                        if (cnt >= max_nbr) return;
+                    }
+                }
+            }
+    out[(size_t)cnt * n] = 0xffffffffu;
+}
+
 struct PosF4 {
     const float4* __restrict__ a;
     __device__ __forceinline__ vec3 operator()(uint32_t i) const { return xyz(a[i]); }
@@ -339,18 +434,16 @@ struct PosF3 {
 
 __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
-                  const uint32_t* __restrict__ vals, const uint32_t* __restrict__ cs,
-                  const uint32_t* __restrict__ ce, const float4* __restrict__ p,
-                  const float4* __restrict__ x0, uint32_t* __restrict__ nbr)
+                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                  const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr)
 {
     const Tile tl = tiles[blockIdx.x];
     const int t = tl.begin + (int)threadIdx.x;
     if (t >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
-    cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF4{p}, PosF4{x0}, nbr + D.nbr_base,
-                        (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
-                        ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2,
-                        D.diameter2, D.max_nbr);
+    cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + D.nbr_base, (uint32_t)D.p_begin, D.p_count,
+                           D.table_base, D.table_size, ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing,
+                           D.cell_spacing2, D.diameter2, D.max_nbr);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -392,8 +485,10 @@ k_hash_keys_arena(const int32_t* __restrict__ pdom, const DomainParams* __restri
 }
 
 __global__ void __launch_bounds__(kBlock)
-k_cell_ranges_arena(const uint32_t* __restrict__ keys, int32_t n, uint32_t sentinel,
-                    uint32_t* __restrict__ cs, uint32_t* __restrict__ ce)
+k_cell_ranges_arena(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                    const float4* __restrict__ p, const float4* __restrict__ x0, int32_t n, uint32_t sentinel,
+                    uint32_t* __restrict__ cs, uint32_t* __restrict__ ce, float4* __restrict__ ps,
+                    float4* __restrict__ x0s)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
     if (t >= n) return;
@@ -404,21 +499,24 @@ k_cell_ranges_arena(const uint32_t* __restrict__ keys, int32_t n, uint32_t senti
         if (t > 0) ce[keys[t - 1]] = (uint32_t)t;
     }
     if (t == n - 1 || keys[t + 1] == sentinel) ce[h] = (uint32_t)(t + 1);
+    const uint32_t id = vals[t];
+    const float4 q = p[id];
+    ps[t] = make_float4(q.x, q.y, q.z, __uint_as_float(id));
+    x0s[t] = x0[id];
 }
 
 __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors_arena(const int32_t* __restrict__ pdom, const DomainParams* __restrict__ doms,
-                        const uint32_t* __restrict__ vals, const uint32_t* __restrict__ cs,
-                        const uint32_t* __restrict__ ce, const float4* __restrict__ p,
-                        const float4* __restrict__ x0, uint32_t* __restrict__ nbr, int32_t n_active)
+                        const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                        const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
+                        int32_t n_active)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
     if (t >= n_active) return;
-    const DomainParams& D = doms[pdom[vals[t]]];
-    cache_neighbors_one((uint32_t)t, vals, cs, ce, PosF4{p}, PosF4{x0}, nbr + D.nbr_base,
-                        (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
-                        ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2,
-                        D.diameter2, D.max_nbr);
+    const DomainParams& D = doms[pdom[__float_as_uint(ps[t].w)]];
+    cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + D.nbr_base, (uint32_t)D.p_begin, D.p_count,
+                           D.table_base, D.table_size, ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing,
+                           D.cell_spacing2, D.diameter2, D.max_nbr);
 }
 
 cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pin, int32_t hw,
@@ -432,10 +530,11 @@ cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pi
     k_hash_keys_arena<<<blocks, kBlock, 0, st>>>(pdom, d.dom, d.p[pin], d.keys, d.vals, hw, sentinel);
     e = radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot, hw, bits, st);
     if (e != cudaSuccess) return e;
-    k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, hw, sentinel, d.cell_start, d.cell_end);
+    k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, d.vals, d.p[pin], d.x0, hw, sentinel, d.cell_start,
+                                                   d.cell_end, d.ps, d.x0s);
     if (n_active > 0)
         k_cache_neighbors_arena<<<(n_active + kBlock - 1) / kBlock, kBlock, 0, st>>>(
-            pdom, d.dom, d.vals, d.cell_start, d.cell_end, d.p[pin], d.x0, d.nbr, n_active);
+            pdom, d.dom, d.cell_start, d.cell_end, d.ps, d.x0s, d.nbr, n_active);
     const int passes = (hw > 1 && bits > 0) ? (bits + 7) / 8 : 0;
     if (launches) *launches += 3 + 3 * (uint64_t)passes;
     return cudaGetLastError();
@@ -453,8 +552,9 @@ cudaError_t launch_cache_neighbors(const Launch& L, int pin)
 {
     if (!L.n_ptiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
-    k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.vals, d.cell_start,
-                                                       d.cell_end, d.p[pin], d.x0, d.nbr);
+    (void)pin;  // positions come sorted from launch_cell_ranges_gather
+    k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.cell_start, d.cell_end, d.ps,
+                                                       d.x0s, d.nbr);
     return cudaGetLastError();
 }
 

@@ -186,9 +186,12 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
         const uint32_t* nb = nbr + D.nbr_base + (i - D.p_begin);
         const int stride = D.p_count;
         const float diam = D.diameter;
+        // the next list entry is requested while this one is processed
+        uint32_t jn = __ldg(nb);
         for (int k = 0; k < D.max_nbr; ++k) {
-            const uint32_t j = __ldg(nb + (size_t)k * stride);
+            const uint32_t j = jn;
             if (j == 0xffffffffu) break;
+            if (k + 1 < D.max_nbr) jn = __ldg(nb + (size_t)(k + 1) * stride);
             const float4 pj4 = pin[j];
             const float denom = wi + pj4.w;
             if (denom <= 0) continue;
@@ -659,6 +662,25 @@ k_grid_normals(const Tile* __restrict__ tiles, const DomainParams* __restrict__ 
     if (a < R && b < R) acc3(acc, tri_n(a, b, a + 1, b, a, b + 1));                 // (a,b).0
     const vec3 n = normalize(acc);
     nrm[i] = make_float4(n.x, n.y, n.z, 0.0f);
+}
+
+// ------------------------------------------------------------------ read-back packing
+__global__ void __launch_bounds__(kBlock) k_pack_xyz(const float4* __restrict__ src, float* __restrict__ dst,
+                                                      int64_t n)
+{
+    const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (i >= n) return;
+    const float4 q = src[i];
+    dst[3 * i] = q.x;
+    dst[3 * i + 1] = q.y;
+    dst[3 * i + 2] = q.z;
+}
+
+cudaError_t launch_pack_xyz(const float4* src, float* dst, int64_t n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_pack_xyz<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ launchers

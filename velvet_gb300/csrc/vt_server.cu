@@ -11,6 +11,14 @@
 // in FIFO order while the budget, the slot table and the active-particle cap allow,
 // rebuild the tile tables if the active set changed, then one frame for every active
 // request with the same kernels as the batched form.
+//
+// Ticks are pipelined: a tick enqueues its frame and then waits only for the previous
+// tick's frame, so the host's retire / admit / table work of tick t runs while frame t-1
+// is on the GPU.  Everything a tick enqueues goes on one stream after the previous frame,
+// so a range released by a request that finished in frame t-1 can be handed to a new
+// request in tick t: the new request's uploads are ordered after the old one's result
+// copy.  Uploads and result copies go through two pinned rings each, alternating by
+// tick parity; ring t%2 is free again once frame t-1 has completed.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -28,19 +36,39 @@ namespace {
 constexpr int kSlotsPerCloth = vt::kGridLraCached;  // attach slots a request may use
 constexpr int kCollidersPerCloth = 8;
 constexpr int kMaxNbr = 64;
-// device bytes per arena particle: x v x0 p0 p1 nrm grest glra (float4), domain id,
-// keys vals + sort temporaries, neighbour lists, cell start/end (3 cells per particle)
-constexpr uint64_t kBytesPerParticle = 8 * 16 + 4 + 4 * 4 + kMaxNbr * 4 + 3 * 2 * 4;
+// device bytes per arena particle: x v x0 p0 p1 nrm grest glra ps x0s (float4), domain id,
+// keys vals + sort temporaries, neighbour lists, cell start/end (3 cells per particle),
+// packed read-back xyz
+constexpr uint64_t kBytesPerParticle = 10 * 16 + 4 + 4 * 4 + kMaxNbr * 4 + 3 * 2 * 4 + 12;
 
 struct Request {
     int64_t id = 0;
-    int32_t frames = 0, done = 0, state = VT_REQ_QUEUED;
+    int32_t frames = 0, state = VT_REQ_QUEUED;
+    int32_t enq = 0;   // frames enqueued
+    int32_t done = 0;  // frames completed on the GPU
     vt::HostSolver h;
     int32_t sid = -1;
     int64_t pb = -1;
     uint32_t n = 0;
+    const float* res_pin = nullptr;  // result in a pinned ring (copied out when complete)
     std::vector<float> result;
 };
+
+// Bump allocator over one pinned host buffer, reset once the copies it fed completed.
+struct PinnedRing {
+    char* base = nullptr;
+    size_t cap = 0, used = 0;
+    void* take(size_t bytes)
+    {
+        const size_t b = (bytes + 255) & ~size_t(255);
+        if (!base || used + b > cap) return nullptr;
+        void* p = base + used;
+        used += b;
+        return p;
+    }
+};
+constexpr size_t kUploadRingBytes = 64u << 20;  // 80 B per admitted particle
+constexpr size_t kResultRingBytes = 32u << 20;  // 12 B per finished particle
 
 // First-fit allocator of [begin, end) ranges in [0, cap).
 struct RangeAlloc {
@@ -107,7 +135,17 @@ struct vt_server {
     int32_t* pdom = nullptr;
     void* staging = nullptr;  // pinned: params, colliders, slots, tile tables
     size_t staging_bytes = 0;
-    cudaEvent_t staged = nullptr, ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t staged = nullptr;
+    cudaEvent_t ev0[2] = {nullptr, nullptr}, ev1[2] = {nullptr, nullptr};  // frame of tick parity
+    PinnedRing up[2], res[2];
+    std::vector<Request*> members[2];    // requests in the frame of tick parity k
+    std::vector<Request*> finishing[2];  // result copies enqueued in the tick of parity k
+    uint64_t frame_particles[2] = {0, 0};
+    bool inflight[2] = {false, false};
+    uint64_t tick_no = 0;
+    cudaStream_t last_stream = nullptr;
+    bool stream_set = false;
+    int32_t n_finishing = 0;
     RangeAlloc alloc;
     std::deque<Request*> queue;
     std::vector<Request*> slot;  // per slot id, nullptr when free
@@ -130,8 +168,12 @@ struct vt_server {
         if (arena) cudaFree(arena);
         if (staging) cudaFreeHost(staging);
         if (staged) cudaEventDestroy(staged);
-        if (ev0) cudaEventDestroy(ev0);
-        if (ev1) cudaEventDestroy(ev1);
+        for (int k = 0; k < 2; ++k) {
+            if (ev0[k]) cudaEventDestroy(ev0[k]);
+            if (ev1[k]) cudaEventDestroy(ev1[k]);
+            if (up[k].base) cudaFreeHost(up[k].base);
+            if (res[k].base) cudaFreeHost(res[k].base);
+        }
     }
 };
 
@@ -170,26 +212,36 @@ vt::FrameArgs frame_args(const vt_server* s, const vt::HostSolver& h)
                          h.P.particle_diameter};
 }
 
-// Uploads a request's state into its arena range and fills its parameter slot.
-vt_status place(vt_server* s, Request* r, cudaStream_t st)
+// Uploads a request's state into its arena range and fills its parameter slot.  The
+// upload images are built in `ring` (pinned; reused once this tick's frame completed);
+// a request larger than a whole ring is uploaded from pageable memory and waited for.
+// Returns VT_ERR_CAPACITY, with nothing done, when the ring has no room left this tick.
+vt_status place(vt_server* s, Request* r, cudaStream_t st, PinnedRing& ring)
 {
     const vt::HostSolver& h = r->h;
     const size_t n = r->n, pb = (size_t)r->pb;
-    std::vector<float4> x(n), v(n), x0(n), grest(n), glra(n);
+    std::vector<float4> own;
+    float4* buf = static_cast<float4*>(ring.take(5 * 16 * n));
+    if (!buf) {
+        if (5 * 16 * n + 256 <= ring.cap) return VT_ERR_CAPACITY;  // fits an emptier ring
+        own.resize(5 * n);
+        buf = own.data();
+    }
+    float4 *x = buf, *v = buf + n, *x0 = buf + 2 * n, *grest = buf + 3 * n, *glra = buf + 4 * n;
     for (size_t i = 0; i < n; ++i) {
         x[i] = make_float4(h.x[3 * i], h.x[3 * i + 1], h.x[3 * i + 2], h.w[i]);
         v[i] = make_float4(h.v[3 * i], h.v[3 * i + 1], h.v[3 * i + 2], 0.0f);
         x0[i] = make_float4(h.x0[3 * i], h.x0[3 * i + 1], h.x0[3 * i + 2], 0.0f);
     }
-    vt::grid_rests(h, grest.data(), glra.data());
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.x + pb, x.data(), 16 * n, cudaMemcpyHostToDevice, st), "upload x");
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.v + pb, v.data(), 16 * n, cudaMemcpyHostToDevice, st), "upload v");
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.x0 + pb, x0.data(), 16 * n, cudaMemcpyHostToDevice, st), "upload x0");
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.grest + pb, grest.data(), 16 * n, cudaMemcpyHostToDevice, st), "upload grest");
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.glra + pb, glra.data(), 16 * n, cudaMemcpyHostToDevice, st), "upload glra");
+    vt::grid_rests(h, grest, glra);
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.x + pb, x, 16 * n, cudaMemcpyHostToDevice, st), "upload x");
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.v + pb, v, 16 * n, cudaMemcpyHostToDevice, st), "upload v");
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.x0 + pb, x0, 16 * n, cudaMemcpyHostToDevice, st), "upload x0");
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.grest + pb, grest, 16 * n, cudaMemcpyHostToDevice, st), "upload grest");
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.glra + pb, glra, 16 * n, cudaMemcpyHostToDevice, st), "upload glra");
     k_fill_i32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s->pdom + pb, (int64_t)n, r->sid);
     VT_TRY_CUDA(cudaGetLastError(), "fill domain ids");
-    VT_TRY_CUDA(cudaStreamSynchronize(st), "upload");  // host vectors go out of scope
+    if (!own.empty()) VT_TRY_CUDA(cudaStreamSynchronize(st), "upload");  // pageable images go out of scope
     s->launches += 1;
 
     const int sid = r->sid;
@@ -345,7 +397,8 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     const size_t cells = ((size_t)cap * 3 * 4 + 255) & ~size_t(255), nbr = (size_t)cap * kMaxNbr * 4;
     const size_t small = M * (sizeof(vt::DomainParams) + kCollidersPerCloth * sizeof(vt::ColliderDev) +
                               2 * 16 * kSlotsPerCloth) + 4 * (M + 1) + 4096 * 4;
-    const size_t total = 8 * a16 + 5 * a4 + hist + 2 * cells + nbr + small +
+    const size_t a12 = ((size_t)cap * 12 + 255) & ~size_t(255);
+    const size_t total = 10 * a16 + 5 * a4 + a12 + hist + 2 * cells + nbr + small +
                          tiles_bytes(cap_pt, sizeof(vt::Tile)) * 2 + tiles_bytes(cap_gt, sizeof(vt::GridTile)) +
                          64 * 256;
     VT_TRY_CUDA(cudaMalloc(&s->arena, total), "cudaMalloc(server arena)");
@@ -354,12 +407,14 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     s->d.x = (float4*)take(a16); s->d.v = (float4*)take(a16); s->d.x0 = (float4*)take(a16);
     s->d.p[0] = (float4*)take(a16); s->d.p[1] = (float4*)take(a16); s->d.nrm = (float4*)take(a16);
     s->d.grest = (float4*)take(a16); s->d.glra = (float4*)take(a16);
+    s->d.ps = (float4*)take(a16); s->d.x0s = (float4*)take(a16);
     s->pdom = (int32_t*)take(a4);
     s->d.keys = (uint32_t*)take(a4); s->d.vals = (uint32_t*)take(a4);
     s->d.keys_tmp = (uint32_t*)take(a4); s->d.vals_tmp = (uint32_t*)take(a4);
     s->d.hist = (uint32_t*)take(hist); s->d.digit_tot = (uint32_t*)take(256 * 4);
     s->d.cell_start = (uint32_t*)take(cells); s->d.cell_end = (uint32_t*)take(cells);
     s->d.nbr = (uint32_t*)take(nbr);
+    s->d.packed = (float*)take(a12);
     s->d.dom = (vt::DomainParams*)take(M * sizeof(vt::DomainParams));
     s->d.col = (vt::ColliderDev*)take(M * kCollidersPerCloth * sizeof(vt::ColliderDev));
     s->d.slots = (float4*)take(M * kSlotsPerCloth * 16);
@@ -380,8 +435,14 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
                       cap_pt * 2 * sizeof(vt::Tile) + cap_gt * sizeof(vt::GridTile) + 16 * 256;
     VT_TRY_CUDA(cudaMallocHost(&s->staging, s->staging_bytes), "cudaMallocHost(server staging)");
     VT_TRY_CUDA(cudaEventCreateWithFlags(&s->staged, cudaEventDisableTiming), "event");
-    VT_TRY_CUDA(cudaEventCreate(&s->ev0), "event");
-    VT_TRY_CUDA(cudaEventCreate(&s->ev1), "event");
+    for (int k = 0; k < 2; ++k) {
+        VT_TRY_CUDA(cudaEventCreate(&s->ev0[k]), "event");
+        VT_TRY_CUDA(cudaEventCreate(&s->ev1[k]), "event");
+        VT_TRY_CUDA(cudaMallocHost((void**)&s->up[k].base, kUploadRingBytes), "cudaMallocHost(upload ring)");
+        s->up[k].cap = kUploadRingBytes;
+        VT_TRY_CUDA(cudaMallocHost((void**)&s->res[k].base, kResultRingBytes), "cudaMallocHost(result ring)");
+        s->res[k].cap = kResultRingBytes;
+    }
     VT_TRY_CUDA(vt::prepare_kernels(), "kernel attributes");
     s->alloc.init(cap);
     s->slot.assign(M, nullptr);
@@ -437,14 +498,31 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
     VT_CHECK(s, VT_ERR_INVALID_ARGUMENT, "NULL server");
     VT_GUARD_BEGIN
     cudaStream_t st = (cudaStream_t)stream;
+    if (s->stream_set && st != s->last_stream)  // the pipeline is ordered by one stream
+        VT_TRY_CUDA(cudaStreamSynchronize(s->last_stream), "previous stream");
+    s->last_stream = st;
+    s->stream_set = true;
+    const int par = (int)(s->tick_no & 1), prev = 1 - par;
     vt_server_tick_info ti{};
-    // 1. retire
+    // 1. retire: requests whose last frame is enqueued; their result copy is ordered after
+    // that frame on the stream, so their range and slot are free for this tick's admissions
     for (int32_t sid = 0; sid < (int32_t)s->slot.size(); ++sid) {
         Request* r = s->slot[sid];
-        if (!r || r->done < r->frames) continue;
-        r->result.resize(3 * (size_t)r->n);
-        VT_TRY_CUDA(cudaMemcpy2DAsync(r->result.data(), 12, s->d.x + r->pb, 16, 12, r->n,
-                                      cudaMemcpyDeviceToHost, st), "read result");
+        if (!r || r->enq < r->frames) continue;
+        float* pk = s->d.packed + 3 * r->pb;
+        VT_TRY_CUDA(vt::launch_pack_xyz(s->d.x + r->pb, pk, (int64_t)r->n, st), "pack result");
+        s->launches += 1;
+        float* dst = static_cast<float*>(s->res[par].take(12 * (size_t)r->n));
+        if (dst) {
+            VT_TRY_CUDA(cudaMemcpyAsync(dst, pk, 12 * (size_t)r->n, cudaMemcpyDeviceToHost, st), "read result");
+            r->res_pin = dst;
+        } else {  // larger than the ring: straight into the request, waited for
+            r->result.resize(3 * (size_t)r->n);
+            VT_TRY_CUDA(cudaMemcpyAsync(r->result.data(), pk, 12 * (size_t)r->n, cudaMemcpyDeviceToHost, st),
+                        "read result");
+            VT_TRY_CUDA(cudaStreamSynchronize(st), "read result");
+            r->res_pin = nullptr;
+        }
         k_fill_i32<<<(unsigned)((r->n + 255) / 256), 256, 0, st>>>(s->pdom + r->pb, (int64_t)r->n, -1);
         VT_TRY_CUDA(cudaGetLastError(), "clear domain ids");
         s->launches += 1;
@@ -452,14 +530,12 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
         s->active_particles -= r->n;
         s->n_active -= 1;
         s->slot[sid] = nullptr;
-        r->state = VT_REQ_DONE;
         r->sid = -1;
-        r->h = vt::HostSolver{};  // release the staging copy
-        s->stats.requests_done += 1;
+        s->finishing[par].push_back(r);
+        s->n_finishing += 1;
         s->tables_dirty = true;
         ti.retired += 1;
     }
-    VT_TRY_CUDA(cudaStreamSynchronize(st), "retire");
     // 2. admit, FIFO
     while (!s->queue.empty()) {
         Request* r = s->queue.front();
@@ -473,9 +549,12 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
         if (pb < 0) break;
         r->sid = sid;
         r->pb = pb;
-        vt_status pr = place(s, r, st);
+        const vt_status pr = place(s, r, st, s->up[par]);
         if (pr != VT_OK) {
             s->alloc.release(pb, r->n);
+            r->sid = -1;
+            r->pb = -1;
+            if (pr == VT_ERR_CAPACITY) break;  // upload ring full: next tick
             return pr;
         }
         s->slot[sid] = r;
@@ -486,30 +565,56 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
         s->tables_dirty = true;
         ti.admitted += 1;
     }
-    // 3. tables, 4. one frame
+    // 3. tables, 4. enqueue one frame for every active request
     if (s->tables_dirty) {
-        vt_status ur = upload_tables(s, st);
+        const vt_status ur = upload_tables(s, st);
         if (ur != VT_OK) return ur;
     }
+    s->members[par].clear();
     if (s->n_active > 0) {
-        VT_TRY_CUDA(cudaEventRecord(s->ev0, st), "event");
-        vt_status fr = run_frame(s, st);
+        VT_TRY_CUDA(cudaEventRecord(s->ev0[par], st), "event");
+        const vt_status fr = run_frame(s, st);
         if (fr != VT_OK) return fr;
-        VT_TRY_CUDA(cudaEventRecord(s->ev1, st), "event");
-        VT_TRY_CUDA(cudaEventSynchronize(s->ev1), "frame");
-        float ms = 0;
-        VT_TRY_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1), "elapsed");
-        ti.frame_ms = ms;
+        VT_TRY_CUDA(cudaEventRecord(s->ev1[par], st), "event");
         for (Request* r : s->slot)
-            if (r) r->done += 1;
-        s->frame_log.emplace_back(ms, s->n_active);
-        s->stats.ticks += 1;
-        s->stats.frames_done += (uint64_t)s->n_active;
-        s->stats.particle_iterations +=
-            (double)s->active_particles * (double)s->cfg.substeps * (double)s->cfg.iterations;
-        s->stats.gpu_ms += ms;
+            if (r) {
+                r->enq += 1;
+                s->members[par].push_back(r);
+            }
+        s->frame_particles[par] = s->active_particles;
+        s->inflight[par] = true;
     }
-    ti.active = s->n_active;
+    // 5. complete the previous tick's frame; its uploads and result copies preceded it
+    if (s->inflight[prev]) {
+        VT_TRY_CUDA(cudaEventSynchronize(s->ev1[prev]), "frame");
+        float ms = 0;
+        VT_TRY_CUDA(cudaEventElapsedTime(&ms, s->ev0[prev], s->ev1[prev]), "elapsed");
+        ti.frame_ms = ms;
+        for (Request* r : s->members[prev]) r->done += 1;
+        const int32_t m = (int32_t)s->members[prev].size();
+        s->frame_log.emplace_back(ms, m);
+        s->stats.ticks += 1;
+        s->stats.frames_done += (uint64_t)m;
+        s->stats.particle_iterations +=
+            (double)s->frame_particles[prev] * (double)s->cfg.substeps * (double)s->cfg.iterations;
+        s->stats.gpu_ms += ms;
+        s->inflight[prev] = false;
+    } else if (!s->finishing[prev].empty()) {
+        VT_TRY_CUDA(cudaStreamSynchronize(st), "result copies");
+    }
+    for (Request* r : s->finishing[prev]) {
+        if (r->res_pin) r->result.assign(r->res_pin, r->res_pin + 3 * (size_t)r->n);
+        r->res_pin = nullptr;
+        r->state = VT_REQ_DONE;
+        r->h = vt::HostSolver{};  // release the staging copy
+        s->stats.requests_done += 1;
+        s->n_finishing -= 1;
+    }
+    s->finishing[prev].clear();
+    s->res[prev].used = 0;
+    s->up[prev].used = 0;
+    s->tick_no += 1;
+    ti.active = s->n_active + s->n_finishing;
     ti.queued = (int32_t)s->queue.size();
     ti.active_particles = s->active_particles;
     if (info) *info = ti;

@@ -575,7 +575,8 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_gpt = A.take<Tile>(gpt.size());
     const bool any_grid = !gt.empty();
     const size_t o_grest = A.take<float4>(any_grid ? N : 0), o_glra = A.take<float4>(any_grid ? N : 0);
-    const size_t o_st = A.take<int32_t>(1 + n_domains);
+    const size_t o_st = A.take<int32_t>(1 + n_domains), o_pk = A.take<float>(3 * (size_t)N);
+    const size_t o_ps = A.take<float4>(N), o_x0s = A.take<float4>(N);
     bytes = A.off;
     VT_CUDA(cudaMalloc(&arena_, A.off), "cudaMalloc(world)");
     char* base = (char*)arena_;
@@ -595,7 +596,8 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     d.dom = AT(DomainParams, o_dom); d.col = AT(ColliderDev, o_col);
     d.ptiles = AT(Tile, o_pt); d.btiles = AT(Tile, o_bt); d.status = AT(int32_t, o_st);
     d.stiles = AT(Tile, o_stt); d.gtiles = AT(GridTile, o_gt); d.gptiles = AT(Tile, o_gpt);
-    d.grest = AT(float4, o_grest); d.glra = AT(float4, o_glra);
+    d.grest = AT(float4, o_grest); d.glra = AT(float4, o_glra); d.packed = AT(float, o_pk);
+    d.ps = AT(float4, o_ps); d.x0s = AT(float4, o_x0s);
 #undef AT
     auto up = [](void* dst, const void* src, size_t bytes_) -> cudaError_t {
         return bytes_ ? cudaMemcpy(dst, src, bytes_, cudaMemcpyHostToDevice) : cudaSuccess;
@@ -827,8 +829,7 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
                      radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot,
                                       n_particles, bits, st),
                      "radix_sort", 3 * (uint64_t)sort_passes);
-            VT_STAGE(ST_CELL_RANGES, launch_cell_ranges(d.keys, n_particles, d.cell_start, d.cell_end, st),
-                     "cell_ranges", 1);
+            VT_STAGE(ST_CELL_RANGES, launch_cell_ranges_gather(d, pc, n_particles, st), "cell_ranges", 1);
             VT_STAGE(ST_CACHE_NEIGHBORS, launch_cache_neighbors(L, pc), "cache_neighbors", pk);
         }
         VT_STAGE(ST_COLLIDE, launch_collide(L, pc, 1 - pc), "collide", pk);

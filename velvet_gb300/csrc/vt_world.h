@@ -139,6 +139,9 @@ struct DeviceArrays {
     Tile* gptiles = nullptr;  // particles of the grid domains (normals)
     GridTile* gtiles = nullptr;
     int32_t* status = nullptr;  // device-side fault flag
+    float* packed = nullptr;    // 3 floats per particle: read-back staging (contiguous xyz)
+    // predicted and initial positions in sorted-slot order, rebuilt with every hash
+    float4 *ps = nullptr, *x0s = nullptr;
 };
 
 // ------------------------------------------------------------------ kernel launchers
@@ -151,6 +154,12 @@ struct Launch {
     int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
     int32_t grid_variant = 0;  // tile shape of the gtiles (kGridShape index)
 };
+
+// xyz of src[0, n) into dst as 3 n contiguous floats, so that a read-back is one
+// contiguous copy instead of a copy of 12-byte rows out of 16-byte ones.
+// Cell start/end of the sorted keys plus ps / x0s (positions in sorted-slot order).
+cudaError_t launch_cell_ranges_gather(const DeviceArrays& d, int pin, int32_t n, cudaStream_t st);
+cudaError_t launch_pack_xyz(const float4* src, float* dst, int64_t n, cudaStream_t st);
 
 // One Jacobi iteration of the grid domains (stretch + attach + bending + ApplyDeltas,
 // optionally Finalize / Predict) with implicit topology and shared-memory tiles.
