@@ -31,6 +31,7 @@ import argparse
 import json
 import math
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -220,6 +221,72 @@ def cpu_reference_solver_single(budget_s: float = 8.0) -> dict:
             "sample": f"VtClothSolverCPU restated: 64x64 cloth, {frames} frames in {secs:.1f} s"}
 
 
+def _cpu_solver_worker(args):
+    """VtClothSolverCPU (restated) on the given cloths of a workload, `frames` frames each;
+    returns (pits, seconds)."""
+    idx, wl_name, seed, frames = args
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle import CpuSolver
+
+    wl = workload(wl_name, seed)
+    pits, secs = 0, 0.0
+    for i in idx:
+        spec = wl.cloths[i]
+        s = CpuSolver(spec)
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            s.simulate(wl.frame_dt, wl.substeps, wl.iterations)
+        secs += time.perf_counter() - t0
+        pits += spec.num_particles * wl.substeps * wl.iterations * frames
+        s.close()
+    return pits, secs
+
+
+def cpu_reference_solver_all_cores(wl_name: str, seed: int) -> dict:
+    """VtClothSolverCPU on every host core, one independent cloth at a time per process,
+    over a size-preserving sample of the workload (cloths are independent, so the cores
+    share nothing): aggregate particle-iterations / wall time."""
+    import multiprocessing as mp
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle
+
+    oracle.cpu_solver_lib()  # build once here, before the workers load it
+    wl = workload(wl_name, seed)
+    cores = os.cpu_count() or 1
+    idx = sample_indices(wl, 150_000 * cores)
+    chunks = [c for c in (idx[k::cores] for k in range(cores)) if c]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(chunks)) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_solver_worker, [(c, wl_name, seed, 2) for c in chunks])
+        wall = time.perf_counter() - t0
+    pits = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    return {"value": pits / busy, "unit": UNIT, "cores": len(chunks), "kind": "port",
+            "sample": f"VtClothSolverCPU restated: {len(idx)} of {len(wl.cloths)} cloths, 2 frames each, "
+                      f"{len(chunks)} processes, {pits / 1e6:.1f} M particle-iterations, slowest process "
+                      f"{busy:.1f} s of simulation ({wall:.1f} s with process start-up)"}
+
+
+def host_info() -> dict:
+    """Core count and CPU model of the host the bench ran on."""
+    model = platform.processor() or platform.machine()
+    try:
+        fields: dict[str, str] = {}
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if ":" in line:
+                k, v = line.split(":", 1)
+                fields.setdefault(k.strip().lower(), v.strip())
+        if "model name" in fields:
+            model = fields["model name"]
+        elif "cpu part" in fields:  # Arm: implementer / part codes (0x41 / 0xd4f = Arm Neoverse V2)
+            model = f"Arm implementer {fields.get('cpu implementer', '?')} part {fields['cpu part']}"
+    except OSError:
+        pass
+    return {"nproc": os.cpu_count(), "cpu_model": model, "machine": platform.machine()}
+
+
 def run_reference(args) -> None:
     rank, world, _ = env_rank()
     if rank != 0:
@@ -387,28 +454,44 @@ def run_serving(args) -> None:
     S, It = 5, 10
     templates: dict[int, object] = {}
 
+    def spec_of(side):
+        return W.ClothSpec(side, 0.02, W.horizontal_cloth(side, 0.02, 0.8), [0, side - 1],
+                           W.static_colliders([W.sphere((0.0, 0.3, 0.0), 0.3), W.plane(0.0)]))
+
     def template(side):
         if side not in templates:
-            spec = W.ClothSpec(side, 0.02, W.horizontal_cloth(side, 0.02, 0.8), [0, side - 1],
-                               W.static_colliders([W.sphere((0.0, 0.3, 0.0), 0.3), W.plane(0.0)]))
+            spec = spec_of(side)
             s = vg.ClothSolver()
             W.build_plain(spec, s)
             templates[side] = (s, spec)
         return templates[side]
 
-    # requests arrive with their cloth already registered (the client's work): build the
-    # payload of every size that can arrive before the timed loop
+    described: dict[int, tuple] = {}
+
+    def submit(srv, side, frames):
+        if args.described:  # the cloth is described; the server builds it on the device
+            if side not in described:
+                spec = spec_of(side)
+                described[side] = (spec, spec.particle_diameter(), spec.colliders(0))
+            spec, d, cols = described[side]
+            return srv.submit_grid(spec.resolution, spec.spacing * spec.resolution, spec.model, d,
+                                   spec.attached, cols, frames)
+        s, _ = template(side)
+        return srv.submit(s, frames)
+
+    # registered requests arrive with their cloth already registered (the client's
+    # work): build the payload of every size that can arrive before the timed loop
     tb = time.perf_counter()
-    for side in sorted(set(int(v) for v in sides)):
-        template(side)
+    if not args.described:
+        for side in sorted(set(int(v) for v in sides)):
+            template(side)
     build_s = time.perf_counter() - tb
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     srv = vg.ClothServer(int(args.budget_gb * (1 << 30)), max_cloths=4096,
                          max_active_particles=args.max_active_particles, substeps=S, iterations=It)
     # warm-up: one small request through the whole path
-    s0, _ = template(16)
-    srv.submit(s0, 3)
+    submit(srv, 16, 3)
     while srv.tick(stream).active or srv.stats().requests_done < 1:
         pass
     base = srv.stats()
@@ -426,8 +509,7 @@ def run_serving(args) -> None:
         info_q = 0
         while backlog and info_q < 2:
             j = backlog.pop(0)
-            s, _ = template(int(sides[j]))
-            srv.submit(s, int(frames[j]))
+            submit(srv, int(sides[j]), int(frames[j]))
             info_q += 1
         info = srv.tick(stream)
         ticks += 1
@@ -442,7 +524,9 @@ def run_serving(args) -> None:
               "backlog_at_end": len(backlog),
               "mean_active_particles": float(np.mean(active_samples)) if active_samples else 0.0,
               "gpu_busy_frac": (st.gpu_ms - base.gpu_ms) / 1000.0 / wall,
-              "payload_build_s_untimed": build_s, "distinct_sizes": len(templates)}
+              "payload_build_s_untimed": build_s, "distinct_sizes": len(templates) or len(described),
+              "submission": "described grid cloths, built on the device at admission" if args.described
+              else "registered solvers (host-built constraint arrays)"}
     srv.close()
 
     # the plain solver, one request at a time, same stream of requests, bounded time
@@ -450,7 +534,7 @@ def run_serving(args) -> None:
     t1 = time.perf_counter()
     j = 0
     while time.perf_counter() - t1 < args.plain_seconds and j < n_req:
-        _, spec = template(int(sides[j]))
+        spec = spec_of(int(sides[j]))
         s = vg.ClothSolver()
         W.build_plain(spec, s)
         d = spec.particle_diameter()
@@ -498,6 +582,8 @@ def main() -> None:
                     help="only run this many frames of the workload and exit (for ncu captures)")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of arrivals")
+    ap.add_argument("--described", action="store_true",
+                    help="serving: submit grid cloths by description (built on the device)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device-memory budget")
     ap.add_argument("--max-active-particles", type=int, default=2_500_000,
                     help="serving: admission stops above this many active particles")
@@ -616,7 +702,8 @@ def main() -> None:
     ncol = sum(len(c.colliders(0)) for c in wl.cloths)
     h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
     d2h = n_tot * 24
-    grid_tile = ["7x31", "15x15", "3x63"][batch.grid_tile()] if batch.grid_tile() >= 0 else None
+    grid_tile = (["7x31", "15x15", "3x63"][batch.grid_tile() % 3] + (" x5/SM" if batch.grid_tile() >= 3 else " x4/SM")
+                 if batch.grid_tile() >= 0 else None)
     batch.close()
 
     # ---- the plain drop-in solver on the same workload, one cloth at a time
@@ -633,10 +720,11 @@ def main() -> None:
         for s, _, _ in solvers:
             s.close()
 
-    cpu, cpu_ref_solver = None, None
+    cpu, cpu_ref_solver, cpu_ref_solver_all = None, None, None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_single(args.workload, args.seed)
         cpu_ref_solver = cpu_reference_solver_single()
+        cpu_ref_solver_all = cpu_reference_solver_all_cores(args.workload, args.seed)
 
     if rank == 0:
         line = {
@@ -658,6 +746,8 @@ def main() -> None:
             "roofline": roofline,
             "cpu_baseline": cpu,
             "cpu_reference_cpu_solver": cpu_ref_solver,
+            "cpu_reference_cpu_solver_all_cores": cpu_ref_solver_all,
+            "host": host_info(),
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

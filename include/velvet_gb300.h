@@ -346,6 +346,28 @@ vt_status vt_server_destroy(vt_server* s);
  * VT_ERR_CAPACITY if the request could never be admitted (larger than the budget). */
 vt_status vt_server_submit(vt_server* s, vt_solver* cloth, int32_t frames, int64_t* request_id);
 
+/* A grid cloth described instead of registered (no reference counterpart; the device
+ * form of GenerateClothMesh + AddCloth + VtClothObjectGPU::Start, Velvet/Scene.hpp:131-168,
+ * Velvet/VtClothSolverGPU.hpp:114-156, Velvet/VtClothObjectGPU.hpp:43-147): vertex (a, b),
+ * a, b in [0, resolution], at cloth_size * (b / resolution - 0.5, -(a / resolution), 0)
+ * placed by `model`; the grid builder's stretch, bending and LRA attachments to the
+ * `attached` vertices.  Admission builds positions, inverse masses and rest lengths on
+ * the device: no per-particle work on the host.  The result equals registering the same
+ * mesh with vt_cloth_add + vt_cloth_build_grid_constraints and vt_server_submit. */
+typedef struct vt_grid_cloth {
+    int32_t        resolution;
+    float          cloth_size;
+    float          model[16];          /* column-major, as vt_cloth_add */
+    float          particle_diameter;  /* AddCloth's diameter, > 0 */
+    const int32_t* attached;           /* at most 4 vertex indices */
+    uint32_t       n_attached;
+} vt_grid_cloth;
+
+/* Queues a described grid cloth; params NULL = vt_params_default. */
+vt_status vt_server_submit_grid(vt_server* s, const vt_grid_cloth* cloth, const vt_params* params,
+                                const vt_sdf_collider* colliders, uint32_t n_colliders, int32_t frames,
+                                int64_t* request_id);
+
 /* Retire requests whose frames are all enqueued, admit queued ones, enqueue one frame
  * for every active request, then wait for the PREVIOUS tick's frame: the host work of a
  * tick overlaps the GPU work of the one before.  `active` counts admitted requests whose
@@ -365,8 +387,8 @@ vt_status vt_server_stats_get(vt_server* s, vt_server_stats* out);
  * The grid-cloth kernel has several tile shapes; on its first frame a solver, batch or
  * server times them on its own cloths and keeps the fastest (decisions are cached per
  * size signature for the process).  The shape never changes a result.  This forces one
- * shape for all handles created or tuned afterwards: 0 = 7x31, 1 = 15x15, 2 = 3x63;
- * -1 returns to autotuning. */
+ * shape for all handles created or tuned afterwards: 0 = 7x31, 1 = 15x15, 2 = 3x63 at
+ * four resident blocks per SM, 3-5 the same shapes at five; -1 returns to autotuning. */
 vt_status vt_tuning_set_grid_tile(int32_t variant);
 /* The shape in use by a solver / batch (after its first frame). */
 vt_status vt_solver_grid_tile(const vt_solver* s, int32_t* variant);

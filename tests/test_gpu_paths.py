@@ -92,9 +92,10 @@ def test_grid_tiles_at_every_edge_case(tile_edge):
     same(g.velocities(), o.velocities(), f"side {tile_edge} velocities")
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", range(6))
 def test_every_grid_tile_shape_gives_the_same_bits(variant):
-    """The autotuner chooses among tile shapes; each must reproduce the oracle exactly."""
+    """The autotuner chooses among tile shapes and occupancies; each must reproduce the
+    oracle exactly."""
     import ctypes as C
 
     assert vg.lib().vt_tuning_set_grid_tile(variant) == 0

@@ -110,6 +110,51 @@ def test_ticks_overlap_host_work_with_the_previous_frame():
         assert np.array_equal(bits(srv.result(rid)), bits(alone(spec, frames, 2, 3)))
 
 
+def submit_described(srv, spec, frames):
+    return srv.submit_grid(spec.resolution, spec.spacing * spec.resolution, spec.model, spec.particle_diameter(),
+                           spec.attached, spec.colliders(0), frames)
+
+
+def test_described_grid_cloths_built_on_the_device_equal_registered_ones():
+    """vt_server_submit_grid builds mesh, inverse masses and rest lengths with a kernel at
+    admission; mixed with host-registered requests, every result has the bits of the same
+    cloth registered on the host and simulated alone."""
+    srv = vg.ClothServer(hbm_budget_bytes=1 << 30, max_cloths=8, substeps=3, iterations=4)
+    plan = [(request(20, 0.5), 5, True), (request(33, 0.53), 4, False), (request(9, 0.55), 6, True),
+            (W.ClothSpec(17, 0.02, W.horizontal_cloth(17, 0.02, 0.45), [0, 8, 16, 280],
+                         request(17).colliders), 3, True)]
+    ids = []
+    for spec, frames, described in plan:
+        if described:
+            rid = submit_described(srv, spec, frames)
+        else:
+            s = registered(spec)
+            rid = srv.submit(s, frames)
+            s.close()
+        ids.append((rid, spec, frames))
+    for _ in range(60):
+        info = srv.tick()
+        if info.active == 0 and info.queued == 0:
+            break
+    for rid, spec, frames in ids:
+        assert srv.poll(rid) == (_abi.REQ_DONE, frames)
+        assert np.array_equal(bits(srv.result(rid)), bits(alone(spec, frames))), f"side {spec.side}"
+
+
+def test_described_grid_cloth_arguments_are_checked():
+    srv = vg.ClothServer(hbm_budget_bytes=1 << 27, max_cloths=2)
+    spec = request(12)
+    with pytest.raises(vg.VtError) as e:
+        srv.submit_grid(11, 0.22, spec.model, spec.particle_diameter(), [0, 1, 2, 3, 4], spec.colliders(0), 1)
+    assert e.value.status == _abi.VT_ERR_CAPACITY  # more than four attach slots
+    with pytest.raises(vg.VtError) as e:
+        srv.submit_grid(11, 0.22, spec.model, spec.particle_diameter(), [144], spec.colliders(0), 1)
+    assert e.value.status == _abi.VT_ERR_INVALID_ARGUMENT  # vertex out of range
+    with pytest.raises(vg.VtError) as e:
+        srv.submit_grid(699, 13.98, spec.model, spec.particle_diameter(), [0], spec.colliders(0), 1)
+    assert e.value.status == _abi.VT_ERR_CAPACITY  # larger than the arena
+
+
 def test_rejects_non_grid_and_oversize():
     srv = vg.ClothServer(hbm_budget_bytes=1 << 27, max_cloths=2)  # ~300k particles of arena
     s = vg.ClothSolver()

@@ -104,6 +104,19 @@ class VtServerStats(C.Structure):
     ]
 
 
+class VtGridCloth(C.Structure):
+    """vt_grid_cloth — a grid cloth described for device-side construction."""
+
+    _fields_ = [
+        ("resolution", C.c_int32),
+        ("cloth_size", C.c_float),
+        ("model", C.c_float * 16),
+        ("particle_diameter", C.c_float),
+        ("attached", C.POINTER(C.c_int32)),
+        ("n_attached", C.c_uint32),
+    ]
+
+
 REQ_QUEUED, REQ_ACTIVE, REQ_DONE = 0, 1, 2
 
 
@@ -173,6 +186,8 @@ SIGNATURES: dict[str, tuple] = {
     "vt_server_create": (I32, [C.POINTER(VtServerConfig), C.POINTER(P)]),
     "vt_server_destroy": (I32, [P]),
     "vt_server_submit": (I32, [P, P, I32, C.POINTER(C.c_int64)]),
+    "vt_server_submit_grid": (I32, [P, C.POINTER(VtGridCloth), C.POINTER(VtParams), P, U32, I32,
+                                    C.POINTER(C.c_int64)]),
     "vt_server_tick": (I32, [P, P, C.POINTER(VtServerTickInfo)]),
     "vt_server_poll": (I32, [P, C.c_int64, PI32, PI32]),
     "vt_server_result": (I32, [P, C.c_int64, P, U32]),

@@ -425,8 +425,8 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
 // particle's LRA rest distances (glra, up to kGridLraCached slots) are evaluated once
 // at registration with the same FP32 operations instead of every iteration: the kernel
 // is bound by instruction issue, HBM is mostly idle.
-template <int kMode, int kTA, int kTB>
-__global__ void __launch_bounds__(kBlock, 4)
+template <int kMode, int kTA, int kTB, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks)
 k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__ doms,
             const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ x,
             float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ grest,
@@ -439,8 +439,10 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     static_assert(kGGA * kGGB == kBlock, "one generator per thread");
     __shared__ float4 sp[kGHA][kGHB];
     __shared__ float4 sst[4][kGGA][kGGB];  // stretch common + fired flag, per type
+    // the generator's four stretch rest lengths are staged in sst[0] at the generator's own
+    // slot (gx * kGGB + gy == tid): the thread reads them before it writes that slot
+    float4* const sgr = &sst[0][0][0];
     __shared__ float4 sbd[4][kGGA][kGGB];  // bending corner corrections + fired flag
-    __shared__ float4 sgr[kBlock];         // the generator's four stretch rest lengths
     __shared__ float4 sgl[kBlock];         // the particle's LRA rest distances
     __shared__ float4 sx[kBlock];          // the particle's position (finalizing modes)
     __shared__ float4 sslot[kGridLraCached];
@@ -488,7 +490,7 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
         const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
         const bool full = gen && X < R && Y < R;
         const float4 pxy = sp[gx][gy];
-        const float4 rest = sgr[tid];
+        const float4 rest = sgr[tid];  // read before sst[0][gx][gy] (the same slot) is written
         vec3 cm;
         float4 r = zero;
         if (gen && Y < R && stretch_common(pxy, sp[gx][gy + 1], rest.x, cm))  // t0: (x,y)-(x,y+1)
@@ -664,6 +666,52 @@ k_grid_normals(const Tile* __restrict__ tiles, const DomainParams* __restrict__ 
     nrm[i] = make_float4(n.x, n.y, n.z, 0.0f);
 }
 
+// ------------------------------------------------------------------ device grid builder
+// VtClothObjectGPU::Start for a grid cloth (Velvet/VtClothObjectGPU.hpp:43-147) without
+// host loops: every particle evaluates its vertex, its inverse mass (0 when its distance
+// to a slot is 0, AddAttach's rule), its LRA rests |slot - x0_i| and, as generator (a, b),
+// the rest lengths of its four stretch constraints from the neighbouring vertices — the
+// values grid_rests reads from the host-built constraint list, by the same operations.
+__global__ void __launch_bounds__(kBlock)
+k_grid_build(float4* __restrict__ x, float4* __restrict__ v, float4* __restrict__ x0,
+             float4* __restrict__ grest, float4* __restrict__ glra, GridBuildArgs g)
+{
+    const int V = g.res + 1;
+    const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+    if (i >= (int64_t)V * V) return;
+    const int a = (int)(i / V), b = (int)(i - (int64_t)a * V), R = g.res;
+    const vec3 p = grid_vertex(a, b, R, g.size, g.model);
+    float w = 1.0f;
+    float r[kGridLraCached] = {0, 0, 0, 0};
+#pragma unroll
+    for (int s = 0; s < kGridLraCached; ++s)
+        if (s < g.ns) {
+            const float dist = length(xyz(g.slot[s]) - p);
+            if (dist == 0) w = 0;
+            r[s] = dist;
+        }
+    float4 gr = make_float4(0, 0, 0, 0);
+    if (b < R) gr.x = length(p - grid_vertex(a, b + 1, R, g.size, g.model));
+    if (a < R) gr.y = length(p - grid_vertex(a + 1, b, R, g.size, g.model));
+    if (a < R && b < R) {
+        gr.z = length(p - grid_vertex(a + 1, b + 1, R, g.size, g.model));
+        gr.w = length(grid_vertex(a, b + 1, R, g.size, g.model) - grid_vertex(a + 1, b, R, g.size, g.model));
+    }
+    x[i] = make_float4(p.x, p.y, p.z, w);
+    x0[i] = make_float4(p.x, p.y, p.z, 0.0f);
+    v[i] = make_float4(0, 0, 0, 0);
+    grest[i] = gr;
+    glra[i] = make_float4(r[0], r[1], r[2], r[3]);
+}
+
+cudaError_t launch_grid_build(const DeviceArrays& d, int64_t pb, const GridBuildArgs& g, cudaStream_t st)
+{
+    const int64_t n = (int64_t)(g.res + 1) * (g.res + 1);
+    k_grid_build<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, st>>>(d.x + pb, d.v + pb, d.x0 + pb,
+                                                                         d.grest + pb, d.glra + pb, g);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ read-back packing
 __global__ void __launch_bounds__(kBlock) k_pack_xyz(const float4* __restrict__ src, float* __restrict__ dst,
                                                       int64_t n)
@@ -725,19 +773,20 @@ cudaError_t launch_solve(const Launch& L, int pin, int pout, int mode)
     return cudaGetLastError();
 }
 
-template <int kMode, int kTA, int kTB>
+template <int kMode, int kTA, int kTB, int kMinBlocks>
 static cudaError_t carveout()
 {
-    return cudaFuncSetAttribute(k_grid_iter<kMode, kTA, kTB>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                cudaSharedmemCarveoutMaxShared);
+    return cudaFuncSetAttribute(k_grid_iter<kMode, kTA, kTB, kMinBlocks>,
+                                cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
 }
 
 template <int kTA, int kTB>
 static cudaError_t carveout_modes()
 {
-    cudaError_t e = carveout<SOLVE_PLAIN, kTA, kTB>();
-    if (e == cudaSuccess) e = carveout<SOLVE_FINALIZE, kTA, kTB>();
-    if (e == cudaSuccess) e = carveout<SOLVE_FINALIZE_PREDICT, kTA, kTB>();
+    cudaError_t e = carveout<SOLVE_PLAIN, kTA, kTB, 4>();
+    if (e == cudaSuccess) e = carveout<SOLVE_PLAIN, kTA, kTB, 5>();
+    if (e == cudaSuccess) e = carveout<SOLVE_FINALIZE, kTA, kTB, 4>();
+    if (e == cudaSuccess) e = carveout<SOLVE_FINALIZE_PREDICT, kTA, kTB, 4>();
     return e;
 }
 
@@ -750,18 +799,20 @@ cudaError_t prepare_kernels()
     return e;
 }
 
-template <int kTA, int kTB>
+// The plain iterations (nine in ten launches) use the variant's occupancy; the finalizing
+// ones always the four-block build.
+template <int kTA, int kTB, int kMinBlocks>
 static void grid_iter_shape(const Launch& L, int pin, int pout, int mode)
 {
     const DeviceArrays& d = *L.d;
 #define VT_GRID_ARGS \
     d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.grest, d.glra, d.slots, d.slots0, d.status
     if (mode == SOLVE_PLAIN)
-        k_grid_iter<SOLVE_PLAIN, kTA, kTB><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+        k_grid_iter<SOLVE_PLAIN, kTA, kTB, kMinBlocks><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
     else if (mode == SOLVE_FINALIZE)
-        k_grid_iter<SOLVE_FINALIZE, kTA, kTB><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+        k_grid_iter<SOLVE_FINALIZE, kTA, kTB, 4><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
     else
-        k_grid_iter<SOLVE_FINALIZE_PREDICT, kTA, kTB><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+        k_grid_iter<SOLVE_FINALIZE_PREDICT, kTA, kTB, 4><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
 #undef VT_GRID_ARGS
 }
 
@@ -769,9 +820,12 @@ cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int mode)
 {
     if (!L.n_gtiles) return cudaSuccess;
     switch (L.grid_variant) {
-    case 1: grid_iter_shape<kGridShape[1].ta, kGridShape[1].tb>(L, pin, pout, mode); break;
-    case 2: grid_iter_shape<kGridShape[2].ta, kGridShape[2].tb>(L, pin, pout, mode); break;
-    default: grid_iter_shape<kGridShape[0].ta, kGridShape[0].tb>(L, pin, pout, mode); break;
+    case 1: grid_iter_shape<kGridShape[1].ta, kGridShape[1].tb, 4>(L, pin, pout, mode); break;
+    case 2: grid_iter_shape<kGridShape[2].ta, kGridShape[2].tb, 4>(L, pin, pout, mode); break;
+    case 3: grid_iter_shape<kGridShape[0].ta, kGridShape[0].tb, 5>(L, pin, pout, mode); break;
+    case 4: grid_iter_shape<kGridShape[1].ta, kGridShape[1].tb, 5>(L, pin, pout, mode); break;
+    case 5: grid_iter_shape<kGridShape[2].ta, kGridShape[2].tb, 5>(L, pin, pout, mode); break;
+    default: grid_iter_shape<kGridShape[0].ta, kGridShape[0].tb, 4>(L, pin, pout, mode); break;
     }
     return cudaGetLastError();
 }

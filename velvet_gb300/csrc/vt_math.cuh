@@ -118,3 +118,16 @@ VT_HD float vt_acosf(float x)
     }
     return (pio2_hi - vt_asin_series(x)) + pio2_lo;
 }
+
+// Vertex (a, b) of GenerateClothMesh (Velvet/Scene.hpp:131-168) for a cloth of side
+// `size`: size * (b / res - 0.5, -(a / res), 0), placed by InitializePositions'
+// model * (v, 1) (Velvet/VtClothSolverGPU.cu:30-34).  Host and device evaluate it with
+// the same operations, so a cloth built on the device has the bits of one registered
+// from host arrays made the same way.
+VT_HD vec3 grid_vertex(int a, int b, int res, float size, const float* model)
+{
+    const float r = (float)res;
+    const float fx = (float)b / r - 0.5f;
+    const float fy = -((float)a / r);
+    return m4v3(model, mk3(size * fx, size * fy, 0.0f), 1.0f);
+}

@@ -52,6 +52,10 @@ struct Request {
     uint32_t n = 0;
     const float* res_pin = nullptr;  // result in a pinned ring (copied out when complete)
     std::vector<float> result;
+    // described grid cloth (vt_server_submit_grid): built on the device at admission,
+    // h holds its parameters, slots and colliders but no particle arrays
+    bool described = false;
+    vt::GridBuildArgs grid{};
 };
 
 // Bump allocator over one pinned host buffer, reset once the copies it fed completed.
@@ -212,38 +216,12 @@ vt::FrameArgs frame_args(const vt_server* s, const vt::HostSolver& h)
                          h.P.particle_diameter};
 }
 
-// Uploads a request's state into its arena range and fills its parameter slot.  The
-// upload images are built in `ring` (pinned; reused once this tick's frame completed);
-// a request larger than a whole ring is uploaded from pageable memory and waited for.
-// Returns VT_ERR_CAPACITY, with nothing done, when the ring has no room left this tick.
-vt_status place(vt_server* s, Request* r, cudaStream_t st, PinnedRing& ring)
+// The request's parameter block, colliders and attach slots in its slot of the host
+// tables (uploaded with the tile tables).
+vt_status fill_slot_tables(vt_server* s, const Request* r)
 {
     const vt::HostSolver& h = r->h;
     const size_t n = r->n, pb = (size_t)r->pb;
-    std::vector<float4> own;
-    float4* buf = static_cast<float4*>(ring.take(5 * 16 * n));
-    if (!buf) {
-        if (5 * 16 * n + 256 <= ring.cap) return VT_ERR_CAPACITY;  // fits an emptier ring
-        own.resize(5 * n);
-        buf = own.data();
-    }
-    float4 *x = buf, *v = buf + n, *x0 = buf + 2 * n, *grest = buf + 3 * n, *glra = buf + 4 * n;
-    for (size_t i = 0; i < n; ++i) {
-        x[i] = make_float4(h.x[3 * i], h.x[3 * i + 1], h.x[3 * i + 2], h.w[i]);
-        v[i] = make_float4(h.v[3 * i], h.v[3 * i + 1], h.v[3 * i + 2], 0.0f);
-        x0[i] = make_float4(h.x0[3 * i], h.x0[3 * i + 1], h.x0[3 * i + 2], 0.0f);
-    }
-    vt::grid_rests(h, grest, glra);
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.x + pb, x, 16 * n, cudaMemcpyHostToDevice, st), "upload x");
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.v + pb, v, 16 * n, cudaMemcpyHostToDevice, st), "upload v");
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.x0 + pb, x0, 16 * n, cudaMemcpyHostToDevice, st), "upload x0");
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.grest + pb, grest, 16 * n, cudaMemcpyHostToDevice, st), "upload grest");
-    VT_TRY_CUDA(cudaMemcpyAsync(s->d.glra + pb, glra, 16 * n, cudaMemcpyHostToDevice, st), "upload glra");
-    k_fill_i32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s->pdom + pb, (int64_t)n, r->sid);
-    VT_TRY_CUDA(cudaGetLastError(), "fill domain ids");
-    if (!own.empty()) VT_TRY_CUDA(cudaStreamSynchronize(st), "upload");  // pageable images go out of scope
-    s->launches += 1;
-
     const int sid = r->sid;
     vt::DomainParams D{};
     D.p_begin = (int32_t)pb;
@@ -271,6 +249,49 @@ vt_status place(vt_server* s, Request* r, cudaStream_t st, PinnedRing& ring)
         s->hslots0[sid * kSlotsPerCloth + k] = make_float4(q0[0], q0[1], q0[2], 0.0f);
     }
     return VT_OK;
+}
+
+// Uploads a request's state into its arena range and fills its parameter slot (a
+// described grid cloth is built there by a kernel instead).  The upload images are built
+// in `ring` (pinned; reused once this tick's frame completed);
+// a request larger than a whole ring is uploaded from pageable memory and waited for.
+// Returns VT_ERR_CAPACITY, with nothing done, when the ring has no room left this tick.
+vt_status place(vt_server* s, Request* r, cudaStream_t st, PinnedRing& ring)
+{
+    const vt::HostSolver& h = r->h;
+    const size_t n = r->n, pb = (size_t)r->pb;
+    if (r->described) {
+        VT_TRY_CUDA(vt::launch_grid_build(s->d, (int64_t)pb, r->grid, st), "grid build");
+        k_fill_i32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s->pdom + pb, (int64_t)n, r->sid);
+        VT_TRY_CUDA(cudaGetLastError(), "fill domain ids");
+        s->launches += 2;
+        return fill_slot_tables(s, r);
+    }
+    std::vector<float4> own;
+    float4* buf = static_cast<float4*>(ring.take(5 * 16 * n));
+    if (!buf) {
+        if (5 * 16 * n + 256 <= ring.cap) return VT_ERR_CAPACITY;  // fits an emptier ring
+        own.resize(5 * n);
+        buf = own.data();
+    }
+    float4 *x = buf, *v = buf + n, *x0 = buf + 2 * n, *grest = buf + 3 * n, *glra = buf + 4 * n;
+    for (size_t i = 0; i < n; ++i) {
+        x[i] = make_float4(h.x[3 * i], h.x[3 * i + 1], h.x[3 * i + 2], h.w[i]);
+        v[i] = make_float4(h.v[3 * i], h.v[3 * i + 1], h.v[3 * i + 2], 0.0f);
+        x0[i] = make_float4(h.x0[3 * i], h.x0[3 * i + 1], h.x0[3 * i + 2], 0.0f);
+    }
+    vt::grid_rests(h, grest, glra);
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.x + pb, x, 16 * n, cudaMemcpyHostToDevice, st), "upload x");
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.v + pb, v, 16 * n, cudaMemcpyHostToDevice, st), "upload v");
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.x0 + pb, x0, 16 * n, cudaMemcpyHostToDevice, st), "upload x0");
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.grest + pb, grest, 16 * n, cudaMemcpyHostToDevice, st), "upload grest");
+    VT_TRY_CUDA(cudaMemcpyAsync(s->d.glra + pb, glra, 16 * n, cudaMemcpyHostToDevice, st), "upload glra");
+    k_fill_i32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s->pdom + pb, (int64_t)n, r->sid);
+    VT_TRY_CUDA(cudaGetLastError(), "fill domain ids");
+    if (!own.empty()) VT_TRY_CUDA(cudaStreamSynchronize(st), "upload");  // pageable images go out of scope
+    s->launches += 1;
+
+    return fill_slot_tables(s, r);
 }
 
 // Tile tables of the active requests + parameter / collider / slot tables -> device.
@@ -486,6 +507,74 @@ vt_status vt_server_submit(vt_server* s, vt_solver* cloth, int32_t frames, int64
     r->frames = frames;
     r->h = h;
     r->n = h.n();
+    s->queue.push_back(r.get());
+    if (request_id) *request_id = r->id;
+    s->reqs[r->id] = std::move(r);
+    return VT_OK;
+    VT_GUARD_END
+}
+
+vt_status vt_server_submit_grid(vt_server* s, const vt_grid_cloth* c, const vt_params* params,
+                                const vt_sdf_collider* colliders, uint32_t n_colliders, int32_t frames,
+                                int64_t* request_id)
+{
+    VT_CHECK(s && c, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    VT_CHECK(frames >= 1, VT_ERR_INVALID_ARGUMENT, "frames must be >= 1");
+    VT_CHECK(c->resolution >= 1 && c->resolution <= 46340, VT_ERR_INVALID_ARGUMENT, "resolution out of range");
+    VT_CHECK(c->particle_diameter > 0, VT_ERR_INVALID_ARGUMENT, "particle_diameter must be > 0");
+    VT_CHECK(c->n_attached <= (uint32_t)kSlotsPerCloth, VT_ERR_CAPACITY, "more than 4 attach slots");
+    VT_CHECK(c->n_attached == 0 || c->attached, VT_ERR_INVALID_ARGUMENT, "attached is NULL");
+    VT_CHECK(n_colliders <= (uint32_t)kCollidersPerCloth, VT_ERR_CAPACITY, "more than 8 colliders");
+    VT_CHECK(n_colliders == 0 || colliders, VT_ERR_INVALID_ARGUMENT, "colliders is NULL");
+    const int32_t V = c->resolution + 1;
+    const int64_t n = (int64_t)V * V;
+    VT_CHECK(n <= s->cap_p, VT_ERR_CAPACITY, "request larger than the device-memory budget");
+    for (uint32_t k = 0; k < c->n_attached; ++k)
+        VT_CHECK(c->attached[k] >= 0 && c->attached[k] < n, VT_ERR_INVALID_ARGUMENT, "attached vertex out of range");
+    for (uint32_t k = 0; k < n_colliders; ++k)
+        VT_CHECK(colliders[k].type >= 0 && colliders[k].type <= 2, VT_ERR_INVALID_ARGUMENT, "unknown collider type");
+    vt_params P;
+    if (params) {
+        P = *params;
+    } else {
+        vt_params_default(&P);
+    }
+    VT_CHECK(P.num_substeps >= 1 && P.num_iterations >= 0 && P.max_num_neighbors >= 1 &&
+                 P.max_num_neighbors <= kMaxNbr && P.interleaved_hash >= 1 && P.delta_time > 0,
+             VT_ERR_INVALID_ARGUMENT, "invalid parameters");
+    VT_GUARD_BEGIN
+    if (s->reqs.empty() && s->queue.empty()) s->interleaved_hash = P.interleaved_hash;
+    VT_CHECK(P.interleaved_hash == s->interleaved_hash, VT_ERR_INVALID_ARGUMENT,
+             "all requests of a server share interleaved_hash");
+    std::unique_ptr<Request> r(new Request());
+    vt::HostSolver& h = r->h;
+    h.P = P;
+    // AddCloth's parameter updates (Velvet/VtClothSolverGPU.hpp:118-125, 148-149)
+    const float d = c->particle_diameter;
+    h.P.num_particles = (uint32_t)n;
+    h.P.particle_diameter = d;
+    h.P.max_speed = 2.0f * d / h.P.delta_time * (float)h.P.num_substeps;
+    h.cell_spacing = d * h.P.hash_cell_size_scalar;
+    h.table_size = 2 * (int32_t)n;
+    h.grid_res = c->resolution;
+    h.grid_slot_begin = 0;
+    h.grid_slot_count = (int32_t)c->n_attached;
+    h.colliders.assign(colliders, colliders + n_colliders);
+    r->grid.res = c->resolution;
+    r->grid.size = c->cloth_size;
+    std::memcpy(r->grid.model, c->model, sizeof(r->grid.model));
+    r->grid.ns = (int32_t)c->n_attached;
+    for (uint32_t k = 0; k < c->n_attached; ++k) {  // GenerateAttach's slots: the attached vertices
+        const vec3 q = grid_vertex(c->attached[k] / V, c->attached[k] % V, c->resolution, c->cloth_size,
+                                           c->model);
+        h.slots.insert(h.slots.end(), {q.x, q.y, q.z});
+        r->grid.slot[k] = make_float4(q.x, q.y, q.z, 0.0f);
+    }
+    h.slots0 = h.slots;
+    r->described = true;
+    r->id = s->next_id++;
+    r->frames = frames;
+    r->n = (uint32_t)n;
     s->queue.push_back(r.get());
     if (request_id) *request_id = r->id;
     s->reqs[r->id] = std::move(r);

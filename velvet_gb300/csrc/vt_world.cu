@@ -185,7 +185,7 @@ int last_tuned_variant()
 
 vt_status tuning_force(int32_t variant)
 {
-    if (variant < -1 || variant >= kGridShapes) {
+    if (variant < -1 || variant >= kGridVariants) {
         set_error("grid tile variant out of range");
         return VT_ERR_INVALID_ARGUMENT;
     }
@@ -302,7 +302,7 @@ vt_status World::autotune(cudaStream_t st)
         VT_CUDA(cudaEventCreate(&e0), "event");
         VT_CUDA(cudaEventCreate(&e1), "event");
         float best_ms = 0;
-        for (int v = 0; v < kGridShapes; ++v) {
+        for (int v = 0; v < kGridVariants; ++v) {
             vt_status r = set_grid_variant(v);
             if (r != VT_OK) return r;
             Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles, n_gptiles, grid_variant};

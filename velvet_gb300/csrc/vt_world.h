@@ -77,11 +77,17 @@ struct GridShape {
 };
 constexpr int kGridShapes = 3;
 constexpr GridShape kGridShape[kGridShapes] = {{7, 31}, {15, 15}, {3, 63}};
+// A tile-kernel variant is a shape and the resident blocks per SM its plain Jacobi
+// iterations are compiled for: variants 0-2 four blocks (64 registers), 3-5 five blocks
+// (48 registers; the shared-memory footprint allows five).  Results never differ.
+constexpr int kGridVariants = 2 * kGridShapes;
+constexpr int grid_shape_of(int variant) { return variant % kGridShapes; }
 constexpr int kGridTA = 7, kGridTB = 31;  // shape 0
 // Tiles of shape `variant` covering the (grid_res+1)^2 grid cloth of domain `dom`.
 inline void grid_tiles_for(std::vector<GridTile>& out, int dom, const DomainParams& D, int variant)
 {
-    const int V = D.grid_res + 1, ta = kGridShape[variant].ta, tb = kGridShape[variant].tb;
+    const int sh = grid_shape_of(variant);
+    const int V = D.grid_res + 1, ta = kGridShape[sh].ta, tb = kGridShape[sh].tb;
     for (int a = 0; a < V; a += ta)
         for (int b = 0; b < V; b += tb)
             out.push_back(GridTile{dom, a, b, D.grid_res, D.p_begin, D.grid_slot_begin, D.grid_slot_count, 0});
@@ -154,6 +160,18 @@ struct Launch {
     int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
     int32_t grid_variant = 0;  // tile shape of the gtiles (kGridShape index)
 };
+
+// One grid cloth built on the device: GenerateClothMesh + AddCloth (positions, inverse
+// masses with AddAttach's zero-distance rule) + the grid builder's rest lengths and LRA
+// rests, written at particle offset pb of x, v, x0, grest, glra.
+struct GridBuildArgs {
+    int32_t res;
+    float size;
+    float model[16];
+    float4 slot[kGridLraCached];  // LRA slot positions (xyz)
+    int32_t ns;                   // <= kGridLraCached
+};
+cudaError_t launch_grid_build(const DeviceArrays& d, int64_t pb, const GridBuildArgs& g, cudaStream_t st);
 
 // xyz of src[0, n) into dst as 3 n contiguous floats, so that a read-back is one
 // contiguous copy instead of a copy of 12-byte rows out of 16-byte ones.

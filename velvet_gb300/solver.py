@@ -338,6 +338,26 @@ class ClothServer:
         self.sizes[rid.value] = cloth.num_particles
         return rid.value
 
+    def submit_grid(self, resolution: int, cloth_size: float, model: np.ndarray, particle_diameter: float,
+                    attached: Sequence[int], colliders: Sequence[VtSdfCollider], frames: int,
+                    params: VtParams | None = None) -> int:
+        """Queues a grid cloth by description (vt_server_submit_grid): the server builds
+        its mesh, inverse masses and rest lengths on the device at admission."""
+        g = _abi.VtGridCloth()
+        g.resolution = resolution
+        g.cloth_size = cloth_size
+        g.model[:] = [float(v) for v in colmajor(model)]
+        g.particle_diameter = particle_diameter
+        at = (C.c_int32 * max(1, len(attached)))(*attached)
+        g.attached = C.cast(at, C.POINTER(C.c_int32))
+        g.n_attached = len(attached)
+        cols = (VtSdfCollider * max(1, len(colliders)))(*colliders)
+        rid = C.c_int64()
+        check(lib().vt_server_submit_grid(self._h, C.byref(g), C.byref(params) if params is not None else None,
+                                          cols, len(colliders), frames, C.byref(rid)), "vt_server_submit_grid")
+        self.sizes[rid.value] = (resolution + 1) ** 2
+        return rid.value
+
     def tick(self, stream=None) -> _abi.VtServerTickInfo:
         info = _abi.VtServerTickInfo()
         check(lib().vt_server_tick(self._h, stream_handle(stream), C.byref(info)), "vt_server_tick")
