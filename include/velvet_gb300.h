@@ -181,6 +181,16 @@ vt_status vt_bend_add(vt_solver* s, const uint32_t* quads, const float* rest_ang
 vt_status vt_cloth_build_grid_constraints(vt_solver* s, int32_t offset, int32_t resolution,
                                           const int32_t* attached, uint32_t num_attached);
 
+/* General bending adjacency (no reference counterpart: GenerateBending pairs only the two
+ * triangles of each grid quad, Velvet/VtClothObjectGPU.hpp:118-132).  For the cloth at
+ * `offset`, every edge shared by exactly two of its triangles gets one bend constraint
+ * over (first triangle's opposite vertex, second triangle's opposite vertex, shared
+ * edge), hinges in order of their first triangle and corner, with the rest angle the
+ * bending kernel measures at the initial positions (so the registered shape is at rest);
+ * degenerate hinges are skipped.  Any triangle mesh; appended to the cloth's bends and
+ * solved by the general (CSR) kernels.  *out_count (may be NULL) = constraints added. */
+vt_status vt_cloth_build_bending_adjacency(vt_solver* s, int32_t offset, uint32_t* out_count);
+
 /* UpdateColliders (:187-205): replaces the collider list (applied in list order). */
 vt_status vt_colliders_set(vt_solver* s, const vt_sdf_collider* colliders, uint32_t count);
 

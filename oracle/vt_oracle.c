@@ -359,6 +359,87 @@ VO_API int vo_build_grid_constraints(vo_solver* s, int32_t offset, int32_t res,
     return 0;
 }
 
+/* General bending adjacency (vt_cloth_build_bending_adjacency; not in the reference,
+ * whose GenerateBending pairs only the two triangles of a grid quad,
+ * VtClothObjectGPU.hpp:118-132): one bend per edge shared by exactly two triangles of the
+ * cloth, hinges ordered by (first triangle, its corner opposite the edge), corners
+ * (first opposite, second opposite, next-next corner, next corner of the first
+ * triangle), rest angle = the dihedral angle solve_bending measures at x0. */
+typedef struct { uint64_t key; int32_t tri, k; } vo_use;
+typedef struct { int32_t tri, k, tri2, k2; } vo_hinge;
+
+static int cmp_use(const void* a, const void* b)
+{
+    const vo_use *x = (const vo_use*)a, *y = (const vo_use*)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    if (x->tri != y->tri) return x->tri < y->tri ? -1 : 1;  /* keeps triangle order */
+    return x->k < y->k ? -1 : (x->k > y->k);
+}
+
+static int cmp_hinge(const void* a, const void* b)
+{
+    const vo_hinge *x = (const vo_hinge*)a, *y = (const vo_hinge*)b;
+    if (x->tri != y->tri) return x->tri < y->tri ? -1 : 1;
+    return x->k < y->k ? -1 : (x->k > y->k);
+}
+
+static float bend_angle(v3 p0, v3 p1, v3 p2, v3 p3)
+{
+    v3 n1 = vcross(vsub(p2, p0), vsub(p3, p0));
+    n1 = vdivs(n1, vdot(n1, n1));
+    v3 n2 = vcross(vsub(p3, p1), vsub(p2, p1));
+    n2 = vdivs(n2, vdot(n2, n2));
+    return vo_acosf(gclamp(vdot(vnormalize(n1), vnormalize(n2)), -1.0f, 1.0f));
+}
+
+VO_API int vo_build_bending_adjacency(vo_solver* s, int32_t offset, uint32_t* out_count)
+{
+    const vo_cloth* c = NULL;
+    for (size_t k = 0; k < s->cloths.n; ++k)
+        if (s->cloths.d[k].offset == offset) c = &s->cloths.d[k];
+    if (!c) return -1;
+    const uint32_t* t = s->tri.d + c->tri_begin;
+    const int32_t ntri = c->tri_count / 3;
+    vo_use* uses = (vo_use*)malloc(sizeof(vo_use) * (3 * (size_t)ntri + 1));
+    vo_hinge* hinges = (vo_hinge*)malloc(sizeof(vo_hinge) * (3 * (size_t)ntri + 1));
+    size_t nu = 0, nh = 0;
+    for (int32_t q = 0; q < ntri; ++q)
+        for (int k = 0; k < 3; ++k) {
+            uint32_t u = t[3 * q + (k + 1) % 3], v = t[3 * q + (k + 2) % 3];
+            uint32_t lo = u < v ? u : v, hi = u < v ? v : u;
+            vo_use e = {((uint64_t)lo << 32) | hi, q, k};
+            uses[nu++] = e;
+        }
+    qsort(uses, nu, sizeof(vo_use), cmp_use);
+    for (size_t i = 0; i < nu;) {
+        size_t j = i;
+        while (j < nu && uses[j].key == uses[i].key) ++j;
+        if (j - i == 2) {
+            vo_hinge g = {uses[i].tri, uses[i].k, uses[i + 1].tri, uses[i + 1].k};
+            hinges[nh++] = g;
+        }
+        i = j;
+    }
+    qsort(hinges, nh, sizeof(vo_hinge), cmp_hinge);
+    uint32_t added = 0;
+    for (size_t h = 0; h < nh; ++h) {
+        const vo_hinge g = hinges[h];
+        uint32_t i0 = t[3 * g.tri + g.k], i3 = t[3 * g.tri + (g.k + 1) % 3], i2 = t[3 * g.tri + (g.k + 2) % 3];
+        uint32_t i1 = t[3 * g.tri2 + g.k2];
+        v3 p0 = s->x0.d[i0], p1 = s->x0.d[i1], p2 = s->x0.d[i2], p3 = s->x0.d[i3];
+        v3 n1 = vcross(vsub(p2, p0), vsub(p3, p0)), n2 = vcross(vsub(p3, p1), vsub(p2, p1));
+        if (vlen(vsub(p3, p2)) < VO_EPSILON || vdot(n1, n1) == 0 || vdot(n2, n2) == 0) continue;
+        float rest = bend_angle(p0, p1, p2, p3);
+        if (!isfinite(rest)) continue;
+        vo_bend_add(s, i0, i1, i2, i3, rest);
+        ++added;
+    }
+    free(uses);
+    free(hinges);
+    if (out_count) *out_count = added;
+    return 0;
+}
+
 VO_API void vo_colliders_set(vo_solver* s, const vt_sdf_collider* c, uint32_t n)
 {
     free(s->col);

@@ -59,6 +59,7 @@ def lib() -> C.CDLL:
             "vo_attach_add": (None, [P, C.c_int32, C.c_int32, C.c_float]),
             "vo_bend_add": (None, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float]),
             "vo_build_grid_constraints": (C.c_int, [P, C.c_int32, C.c_int32, P, C.c_uint32]),
+            "vo_build_bending_adjacency": (C.c_int, [P, C.c_int32, C.POINTER(C.c_uint32)]),
             "vo_colliders_set": (None, [P, P, C.c_uint32]),
             "vo_simulate": (None, [P, C.c_float, C.c_int32, C.c_int32, C.c_float, C.c_float,
                                    C.c_float, C.c_float]),
@@ -215,6 +216,11 @@ class Oracle:
         at = np.ascontiguousarray(list(attached), np.int32)
         r = lib().vo_build_grid_constraints(self.h, offset, resolution, _p(at) if at.size else None, at.size)
         assert r == 0
+
+    def build_bending_adjacency(self, offset):
+        n = C.c_uint32()
+        assert lib().vo_build_bending_adjacency(self.h, offset, C.byref(n)) == 0
+        return n.value
 
     def update_colliders(self, cols):
         arr = (VtSdfCollider * max(1, len(cols)))(*cols)

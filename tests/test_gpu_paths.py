@@ -126,6 +126,56 @@ def test_many_lra_slots_recompute_their_rests(n_slots):
     same(g.velocities(), o.velocities(), f"{n_slots} LRA slots velocities")
 
 
+def checkerboard_mesh(res, size):
+    """A grid whose quad diagonals alternate direction: not the reference's mesh."""
+    verts, _ = W.grid_mesh(res, size)
+    V = res + 1
+    tris = []
+    for a in range(res):
+        for b in range(res):
+            p, q, r, s = a * V + b, (a + 1) * V + b, a * V + b + 1, (a + 1) * V + b + 1
+            tris += [p, q, r, r, q, s] if (a + b) % 2 == 0 else [p, q, s, p, s, r]
+    return verts, np.array(tris, np.uint32)
+
+
+def unique_edges(idx):
+    e = set()
+    for t in idx.reshape(-1, 3):
+        for k in range(3):
+            u, v = int(t[k]), int(t[(k + 1) % 3])
+            e.add((min(u, v), max(u, v)))
+    return np.array(sorted(e), np.int32)
+
+
+@pytest.mark.parametrize("mesh", ["grid", "checkerboard"])
+def test_general_bending_adjacency_matches_the_oracle(mesh):
+    """vt_cloth_build_bending_adjacency (a hinge per interior edge, rest angle measured at
+    the initial shape) built by the library and by the oracle, solved by the CSR kernels."""
+    res = 14
+    spec = spec_of(res + 1, 0.5)
+    if mesh == "grid":
+        verts, idx = spec.mesh()
+    else:
+        verts, idx = checkerboard_mesh(res, 0.02 * res)
+    o, g = Oracle(), vg.ClothSolver()
+    counts = []
+    for s in (o, g):
+        off = s.add_cloth(verts, idx, spec.model, spec.particle_diameter())
+        if mesh == "grid":
+            s.build_grid_constraints(off, res, spec.attached)
+        else:
+            e = unique_edges(idx)
+            x0 = s.positions()
+            rest = np.sqrt(((x0[e[:, 0]] - x0[e[:, 1]]).astype(np.float32) ** 2).sum(1)).astype(np.float32)
+            s.add_stretch(e, rest)
+        counts.append(s.build_bending_adjacency(off))
+        s.update_colliders(spec.colliders(0))
+    assert counts[0] == counts[1] == res * res + 2 * res * (res - 1)
+    run_frames([o, g], spec, 6)
+    same(g.positions(), o.positions(), f"{mesh} + adjacency bending")
+    same(g.velocities(), o.velocities(), f"{mesh} + adjacency bending velocities")
+
+
 @pytest.mark.parametrize("case", ["no_self_collision", "zero_iterations", "hash_every_substep",
                                   "bend_compliance", "no_friction", "relaxation", "max_neighbors_8"])
 def test_schedule_branches(case):

@@ -234,3 +234,38 @@ def test_hash_objects_against_python_restatement():
         assert col[: len(want)] == want
         if len(want) < mn:
             assert col[len(want)] == 0xFFFFFFFF
+
+
+@pytest.mark.parametrize("res", [1, 2, 5])
+def test_bending_adjacency_on_a_flat_grid(res):
+    """Every interior edge of the grid mesh is a hinge: the R^2 quad diagonals the
+    reference bends plus the 2R(R-1) edges between quads; flat, so every rest angle is 0."""
+    verts, idx = W.grid_mesh(res, 0.02 * res)
+    o = Oracle()
+    off = o.add_cloth(verts, idx, np.eye(4), 0.03)
+    assert o.build_bending_adjacency(off) == res * res + 2 * res * (res - 1)
+    ints, rest = o.constraints(2)
+    assert np.all(rest == 0.0)
+    quads = ints.reshape(-1, 4)
+    # the first hinge is the first quad's diagonal, with the reference's corner order
+    V = res + 1
+    assert quads[0].tolist() == [0, V + 1, 1, V]
+    o.close()
+
+
+def test_bending_adjacency_known_fold_and_non_manifold_edges():
+    # two triangles folded at 90 degrees along the edge (1, 2)
+    verts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.5, 0.5, 1]], np.float32)
+    o = Oracle()
+    off = o.add_cloth(verts, np.array([0, 1, 2, 2, 1, 3], np.uint32), np.eye(4), 0.03)
+    assert o.build_bending_adjacency(off) == 1
+    ints, rest = o.constraints(2)
+    assert ints.tolist() == [0, 3, 2, 1]
+    assert abs(float(rest[0]) - math.pi / 2) < 1e-6
+    o.close()
+    # an edge shared by three triangles is no hinge; nor are boundary edges
+    verts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.5, 0.5, 1], [0.5, 0.5, -1]], np.float32)
+    o = Oracle()
+    off = o.add_cloth(verts, np.array([0, 1, 2, 2, 1, 3, 1, 2, 4], np.uint32), np.eye(4), 0.03)
+    assert o.build_bending_adjacency(off) == 0
+    o.close()

@@ -154,6 +154,7 @@ SIGNATURES: dict[str, tuple] = {
     "vt_attach_generate_lra": (I32, [P, I32, U32, I32, U32]),
     "vt_bend_add": (I32, [P, P, P, U32]),
     "vt_cloth_build_grid_constraints": (I32, [P, I32, I32, P, U32]),
+    "vt_cloth_build_bending_adjacency": (I32, [P, I32, PU32]),
     "vt_colliders_set": (I32, [P, P, U32]),
     "vt_simulate": (I32, [P, F32, I32, I32, F32, F32, F32, F32, P]),
     "vt_solver_sync": (I32, [P]),

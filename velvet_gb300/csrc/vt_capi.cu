@@ -1,5 +1,6 @@
 // vt_capi.cu — extern "C" entry points of the plain solver and the spatial hash
 // (declared in include/velvet_gb300.h).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -433,6 +434,68 @@ vt_status vt_cloth_build_grid_constraints(vt_solver* s, int32_t offset, int32_t 
             h.grid_slot_count = (int32_t)nat;
         }
     }
+    return VT_OK;
+    VT_GUARD_END
+}
+
+vt_status vt_cloth_build_bending_adjacency(vt_solver* s, int32_t offset, uint32_t* out_count)
+{
+    VT_CHECK(s, VT_ERR_INVALID_ARGUMENT, "NULL solver");
+    const ClothRec* c = nullptr;
+    for (const ClothRec& r : s->h.cloths)
+        if (r.offset == offset) c = &r;
+    VT_CHECK(c, VT_ERR_NOT_FOUND, "no cloth starts at this offset");
+    VT_GUARD_BEGIN
+    const ClothRec cl = *c;
+    vt_status st = make_topology_change(s);
+    if (st != VT_OK) return st;
+    HostSolver& h = s->h;
+    const uint32_t* t = h.tri.data() + 3 * (size_t)cl.tri_begin;
+    // every edge (key = the smaller and larger vertex) with the triangles and corners
+    // that contain it, in triangle order; an edge of exactly two triangles is a hinge
+    struct Use {
+        uint64_t key;
+        int32_t tri, k;  // opposite corner k of triangle tri
+    };
+    std::vector<Use> uses;
+    uses.reserve(3 * (size_t)cl.tri_count);
+    for (int32_t q = 0; q < cl.tri_count; ++q)
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t u = t[3 * q + (k + 1) % 3], v = t[3 * q + (k + 2) % 3];
+            uses.push_back({((uint64_t)std::min(u, v) << 32) | std::max(u, v), q, k});
+        }
+    std::stable_sort(uses.begin(), uses.end(), [](const Use& a, const Use& b) { return a.key < b.key; });
+    struct Hinge {
+        int32_t tri, k, tri2, k2;
+    };
+    std::vector<Hinge> hinges;
+    for (size_t i = 0; i < uses.size();) {
+        size_t j = i;
+        while (j < uses.size() && uses[j].key == uses[i].key) ++j;
+        if (j - i == 2) hinges.push_back({uses[i].tri, uses[i].k, uses[i + 1].tri, uses[i + 1].k});
+        i = j;
+    }
+    std::sort(hinges.begin(), hinges.end(),
+              [](const Hinge& a, const Hinge& b) { return a.tri != b.tri ? a.tri < b.tri : a.k < b.k; });
+    auto X0 = [&](uint32_t i) { const size_t q = 3 * (size_t)i; return mk3(h.x0[q], h.x0[q + 1], h.x0[q + 2]); };
+    uint32_t added = 0;
+    for (const Hinge& g : hinges) {
+        // corners as GenerateBending orders a quad: p0 the first triangle's opposite
+        // vertex, p1 the second's, p2-p3 the shared edge with p3 the first triangle's next
+        // corner after p0 (VtClothObjectGPU.hpp:118-132 for a grid quad)
+        const uint32_t i0 = t[3 * g.tri + g.k], i3 = t[3 * g.tri + (g.k + 1) % 3], i2 = t[3 * g.tri + (g.k + 2) % 3];
+        const uint32_t i1 = t[3 * g.tri2 + g.k2];
+        const vec3 p0 = X0(i0), p1 = X0(i1), p2 = X0(i2), p3 = X0(i3);
+        const vec3 n1 = cross(p2 - p0, p3 - p0), n2 = cross(p3 - p1, p2 - p1);
+        if (length(p3 - p2) < VT_EPSILON || dot(n1, n1) == 0 || dot(n2, n2) == 0) continue;  // degenerate
+        const float rest = bend_angle(p0, p1, p2, p3);
+        if (!std::isfinite(rest)) continue;
+        h.bd_idx.insert(h.bd_idx.end(), {i0, i1, i2, i3});
+        h.bd_rest.push_back(rest);
+        ++added;
+    }
+    h.grid_res = -1;
+    if (out_count) *out_count = added;
     return VT_OK;
     VT_GUARD_END
 }

@@ -131,3 +131,16 @@ VT_HD vec3 grid_vertex(int a, int b, int res, float size, const float* model)
     const float fy = -((float)a / r);
     return m4v3(model, mk3(size * fx, size * fy, 0.0f), 1.0f);
 }
+
+// The dihedral angle SolveBending_Kernel (Velvet/VtClothSolverGPU.cu:117-189) measures for
+// corners (p0, p1, p2, p3), shared edge p2-p3, with its operations (each normal divided by
+// its squared length, then normalised; acos of the clamped dot): the rest angle that
+// makes a registered configuration an equilibrium of the constraint.
+VT_HD float bend_angle(vec3 p0, vec3 p1, vec3 p2, vec3 p3)
+{
+    vec3 n1 = cross(p2 - p0, p3 - p0);
+    n1 = n1 / dot(n1, n1);
+    vec3 n2 = cross(p3 - p1, p2 - p1);
+    n2 = n2 / dot(n2, n2);
+    return vt_acosf(gclamp(dot(normalize(n1), normalize(n2)), -1.0f, 1.0f));
+}

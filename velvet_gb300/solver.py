@@ -124,6 +124,13 @@ class ClothSolver:
                                                     _ptr(at) if at.size else None, at.size),
               "vt_cloth_build_grid_constraints")
 
+    def build_bending_adjacency(self, offset: int) -> int:
+        """One bend per interior edge of the cloth at `offset`; returns how many."""
+        n = C.c_uint32()
+        check(lib().vt_cloth_build_bending_adjacency(self._h, offset, C.byref(n)),
+              "vt_cloth_build_bending_adjacency")
+        return n.value
+
     def update_colliders(self, colliders: Sequence[VtSdfCollider]) -> None:
         arr = (VtSdfCollider * max(1, len(colliders)))(*colliders)
         check(lib().vt_colliders_set(self._h, arr, len(colliders)), "vt_colliders_set")
