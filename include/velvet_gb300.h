@@ -393,6 +393,38 @@ vt_status vt_server_result(vt_server* s, int64_t request_id, float* dst, uint32_
 
 vt_status vt_server_stats_get(vt_server* s, vt_server_stats* out);
 
+/* ------------------------------------------------------------------ headless rendering
+ * The particles drawn as shaded spheres into an RGBA8 image by CUDA kernels, the
+ * counterpart of Velvet's ParticleGeometryRenderer + _InstancedParticle shaders
+ * (Velvet/ParticleGeometryRenderer.hpp, Velvet/Assets/Shader/_InstancedParticle.*):
+ * each particle is a screen-space sphere impostor of radius particle_radius (the
+ * reference draws diameter / 2), eye-space normal (u, v, sqrt(1 - u^2 - v^2)) over the
+ * billboard, nearest surface wins, lit by ambient + max(0, N . light_dir) times tint,
+ * gamma 2 (no graphics API exists on the target machines; no shadow map).
+ * view / projection are column-major (glm::lookAt / glm::perspective: a symmetric
+ * frustum); row 0 of the image is the top; pixels no particle covers get `background`. */
+typedef struct vt_render_params {
+    uint32_t width, height;
+    float    view[16], projection[16];
+    float    z_near;                /* particles nearer than this are not drawn */
+    float    particle_radius;       /* world units */
+    float    light_dir[3];          /* world space, towards the light, unit length */
+    float    tint[3];               /* 0.2, 0.3, 0.6 in the reference */
+    float    ambient;               /* 0.3 in the reference */
+    uint32_t background;            /* RGBA8, red in the low byte */
+} vt_render_params;
+
+/* glm::lookAt (right-handed) and glm::perspective (depth -1..1) into column-major arrays. */
+vt_status vt_camera_look_at(const float eye[3], const float center[3], const float up[3], float view[16]);
+vt_status vt_camera_perspective(float fov_y_radians, float aspect, float z_near, float z_far, float proj[16]);
+
+/* Renders the current positions of a solver (after its first simulate) or of every cloth
+ * of a batch into rgba[width * height] (host or device-addressable memory). */
+vt_status vt_solver_render(vt_solver* s, const vt_render_params* rp, uint32_t* rgba, int32_t dst_on_device,
+                           void* stream);
+vt_status vt_batch_render(vt_batch* b, const vt_render_params* rp, uint32_t* rgba, int32_t dst_on_device,
+                          void* stream);
+
 /* ------------------------------------------------------------------ tuning
  * The grid-cloth kernel has several tile shapes; on its first frame a solver, batch or
  * server times them on its own cloths and keeps the fastest (decisions are cached per

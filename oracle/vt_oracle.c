@@ -440,6 +440,65 @@ VO_API int vo_build_bending_adjacency(vo_solver* s, int32_t offset, uint32_t* ou
     return 0;
 }
 
+/* Headless sphere-impostor rendering (vt_solver_render; the library's own feature, the
+ * CUDA counterpart of the reference's _InstancedParticle shaders, which need a graphics
+ * API): the per-particle pixel box and the per-pixel depth|colour key restated with the
+ * same operations, the visible key being the minimum over particles. */
+VO_API void vo_render(const float* xyz, uint32_t n, const vt_render_params* rp, uint32_t* rgba)
+{
+    const size_t npix = (size_t)rp->width * rp->height;
+    uint64_t* z = (uint64_t*)malloc(sizeof(uint64_t) * (npix ? npix : 1));
+    for (size_t k = 0; k < npix; ++k) z[k] = ~0ull;
+    const float W = (float)rp->width, H = (float)rp->height, R = rp->particle_radius;
+    const float* Vm = rp->view;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float xv[4] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 1.0f};
+        float pe4[4];
+        m4v4(Vm, xv, pe4);
+        const v3 pe = V(pe4[0], pe4[1], pe4[2]);
+        if (!(pe.z < -rp->z_near)) continue;
+        const float inv = 1.0f / (-pe.z);
+        const float sx = rp->projection[0] * inv, sy = rp->projection[5] * inv;
+        const float cx = pe.x * sx, cy = pe.y * sy;
+        const float px = (cx * 0.5f + 0.5f) * W, py = (0.5f - cy * 0.5f) * H;
+        const float rx = R * sx * 0.5f * W, ry = R * sy * 0.5f * H;
+        const float lx = px - rx, hx = px + rx, ly = py - ry, hy = py + ry;
+        if (!(lx <= W - 1.0f && hx >= 0.0f && ly <= H - 1.0f && hy >= 0.0f)) continue;
+        const int x0 = lx > 0.0f ? (int)floorf(lx) : 0;
+        const int x1 = hx < W - 1.0f ? (int)ceilf(hx) : (int)rp->width - 1;
+        const int y0 = ly > 0.0f ? (int)floorf(ly) : 0;
+        const int y1 = hy < H - 1.0f ? (int)ceilf(hy) : (int)rp->height - 1;
+        for (int j = y0; j <= y1; ++j)
+            for (int k = x0; k <= x1; ++k) {
+                const float nx = ((float)k + 0.5f) / W * 2.0f - 1.0f;
+                const float ny = 1.0f - ((float)j + 0.5f) / H * 2.0f;
+                const float u = (nx - cx) / (sx * R), v = (ny - cy) / (sy * R);
+                const float r2 = u * u + v * v;
+                if (!(r2 <= 1.0f)) continue;
+                const float nz = sqrtf(1.0f - r2);
+                float depth = -(pe.z + nz * R);
+                if (!(depth > 0.0f)) depth = 0.0f;
+                const v3 nw = V((Vm[0] * u + Vm[1] * v) + Vm[2] * nz, (Vm[4] * u + Vm[5] * v) + Vm[6] * nz,
+                                (Vm[8] * u + Vm[9] * v) + Vm[10] * nz);
+                const float ndl = vdot(nw, V(rp->light_dir[0], rp->light_dir[1], rp->light_dir[2]));
+                const float lit = rp->ambient + (ndl > 0.0f ? ndl : 0.0f);
+                uint32_t col = 0xff000000u;
+                for (int c = 0; c < 3; ++c) {
+                    float q = rp->tint[c] * lit;
+                    q = q < 0.0f ? 0.0f : (q > 1.0f ? 1.0f : q);
+                    col |= (uint32_t)(sqrtf(q) * 255.0f + 0.5f) << (8 * c);
+                }
+                uint32_t bits;
+                memcpy(&bits, &depth, 4);
+                const uint64_t key = ((uint64_t)bits << 32) | col;
+                uint64_t* zp = &z[(size_t)j * rp->width + k];
+                if (key < *zp) *zp = key;
+            }
+    }
+    for (size_t k = 0; k < npix; ++k) rgba[k] = z[k] == ~0ull ? rp->background : (uint32_t)z[k];
+    free(z);
+}
+
 VO_API void vo_colliders_set(vo_solver* s, const vt_sdf_collider* c, uint32_t n)
 {
     free(s->col);

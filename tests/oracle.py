@@ -60,6 +60,7 @@ def lib() -> C.CDLL:
             "vo_bend_add": (None, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float]),
             "vo_build_grid_constraints": (C.c_int, [P, C.c_int32, C.c_int32, P, C.c_uint32]),
             "vo_build_bending_adjacency": (C.c_int, [P, C.c_int32, C.POINTER(C.c_uint32)]),
+            "vo_render": (None, [P, C.c_uint32, P, P]),
             "vo_colliders_set": (None, [P, P, C.c_uint32]),
             "vo_simulate": (None, [P, C.c_float, C.c_int32, C.c_int32, C.c_float, C.c_float,
                                    C.c_float, C.c_float]),
@@ -308,4 +309,12 @@ def hash_objects(pos: np.ndarray, orig: np.ndarray, cell_spacing: float, table_s
     lib().vo_hash_objects(_p(out["particle_hash"]), _p(out["particle_index"]), _p(out["cell_start"]),
                           _p(ce), _p(out["neighbors"]), _p(pos), _p(orig), C.byref(hp))
     out["cell_end"] = ce[:table_size]
+    return out
+
+
+def render(positions, rp):
+    """The oracle's restatement of vt_solver_render on (n, 3) float32 positions."""
+    x = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    out = np.empty((rp.height, rp.width), np.uint32)
+    lib().vo_render(_p(x), x.shape[0], C.byref(rp), _p(out))
     return out

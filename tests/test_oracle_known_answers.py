@@ -269,3 +269,35 @@ def test_bending_adjacency_known_fold_and_non_manifold_edges():
     off = o.add_cloth(verts, np.array([0, 1, 2, 2, 1, 3, 1, 2, 4], np.uint32), np.eye(4), 0.03)
     assert o.build_bending_adjacency(off) == 0
     o.close()
+
+
+def test_render_single_particle_known_answers():
+    """The renderer's restatement: one sphere straight ahead covers a disc of the
+    projected radius around the image centre, lit head-on where the light comes from
+    the camera; the rest is background."""
+    import velvet_gb300 as vg
+
+    W_, H_ = 64, 48
+    rp = vg.render_params(W_, H_, eye=(0, 0, 2), target=(0, 0, 0), particle_radius=0.1,
+                          light_dir=(0, 0, 1), ambient=0.0, tint=(1.0, 0.5, 0.25), background=0xFF000000)
+    img = oracle.render(np.zeros((1, 3), np.float32), rp)
+    bg = img == 0xFF000000
+    # projected radius in pixels: R * f / d * H / 2 with f = 1 / tan(22.5 deg)
+    r_px = 0.1 * (1 / math.tan(math.radians(22.5))) / 2.0 * H_ / 2
+    covered = int((~bg).sum())
+    assert abs(covered - math.pi * r_px * r_px) < 2 * math.pi * r_px + 4
+    # the pixel nearest the centre: its normal's z (the lighting term) from its offset
+    j, i = H_ // 2, W_ // 2
+    f = 1 / math.tan(math.radians(22.5))
+    u = ((i + 0.5) / W_ * 2 - 1) / (f / (W_ / H_) / 2 * 0.1)
+    v = (1 - (j + 0.5) / H_ * 2) / (f / 2 * 0.1)
+    nz = math.sqrt(1 - u * u - v * v)
+    c = int(img[j, i])
+    for ch, tint in enumerate((1.0, 0.5, 0.25)):
+        assert abs(((c >> (8 * ch)) & 0xFF) - 255 * math.sqrt(tint * nz)) <= 1.0
+    assert bg[0, 0] and bg[-1, -1]
+    # a nearer particle hides a farther one behind it
+    two = np.array([[0, 0, 0], [0, 0, 0.5]], np.float32)
+    rp.tint[:] = [1.0, 1.0, 1.0]
+    img2 = oracle.render(two, rp)
+    assert (img2 != 0xFF000000).sum() > covered  # the nearer sphere projects larger

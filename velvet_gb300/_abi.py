@@ -117,6 +117,18 @@ class VtGridCloth(C.Structure):
     ]
 
 
+class VtRenderParams(C.Structure):
+    """vt_render_params — headless sphere-impostor rendering of the particles."""
+
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32),
+        ("view", C.c_float * 16), ("projection", C.c_float * 16),
+        ("z_near", C.c_float), ("particle_radius", C.c_float),
+        ("light_dir", C.c_float * 3), ("tint", C.c_float * 3), ("ambient", C.c_float),
+        ("background", C.c_uint32),
+    ]
+
+
 REQ_QUEUED, REQ_ACTIVE, REQ_DONE = 0, 1, 2
 
 
@@ -196,6 +208,10 @@ SIGNATURES: dict[str, tuple] = {
     "vt_tuning_set_grid_tile": (I32, [I32]),
     "vt_solver_grid_tile": (I32, [P, PI32]),
     "vt_batch_grid_tile": (I32, [P, PI32]),
+    "vt_camera_look_at": (I32, [PF, PF, PF, PF]),
+    "vt_camera_perspective": (I32, [F32, F32, F32, F32, PF]),
+    "vt_solver_render": (I32, [P, C.POINTER(VtRenderParams), P, I32, P]),
+    "vt_batch_render": (I32, [P, C.POINTER(VtRenderParams), P, I32, P]),
     "vt_profiler_enable": (I32, [I32]),
     "vt_profiler_reset": (I32, []),
     "vt_profiler_read": (I32, [C.POINTER(VtStageTime), U32, PU32]),

@@ -256,6 +256,16 @@ vt_status vt_batch_all_get(vt_batch* b, int32_t what, float* dst, int32_t on_dev
     return VT_OK;
 }
 
+vt_status vt_batch_render(vt_batch* b, const vt_render_params* rp, uint32_t* rgba, int32_t dst_on_device,
+                          void* stream)
+{
+    VT_CHECK(b && rp && rgba, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    VT_CHECK(vt::render_params_valid(*rp), VT_ERR_INVALID_ARGUMENT, "invalid render parameters");
+    VT_CHECK(b->world.built() && !b->dirty, VT_ERR_STATE, "render after the first simulate");
+    return vt::render_to(b->world.d.x, (int64_t)b->world.n_particles, *rp, rgba, dst_on_device != 0,
+                         (cudaStream_t)stream, &b->world.launches);
+}
+
 vt_status vt_batch_launch_count(const vt_batch* b, uint64_t* out)
 {
     VT_CHECK(b && out, VT_ERR_INVALID_ARGUMENT, "NULL argument");

@@ -169,6 +169,11 @@ struct SolverImpl {
 // Copies x, v and inverse mass from the device back into the host staging.
 vt_status pull_state(SolverImpl* s);
 
+// Headless rendering (vt_render.cu): parameter check, and x[0, n) rendered into dst.
+bool render_params_valid(const vt_render_params& rp);
+vt_status render_to(const float4* x, int64_t n, const vt_render_params& rp, uint32_t* dst, bool dst_on_device,
+                    cudaStream_t st, uint64_t* launches);
+
 ColliderDev collider_to_device(const vt_sdf_collider& c);
 
 // Grid tile shape to use: the forced one (vt_tuning_set), else `tuned`.

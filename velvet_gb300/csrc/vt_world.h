@@ -173,6 +173,10 @@ struct GridBuildArgs {
 };
 cudaError_t launch_grid_build(const DeviceArrays& d, int64_t pb, const GridBuildArgs& g, cudaStream_t st);
 
+// Splats x[0, n) into rgba (vt_render.cu); zbuf: width * height 64-bit depth|colour keys.
+cudaError_t launch_render(const float4* x, int64_t n, const vt_render_params& rp, unsigned long long* zbuf,
+                          uint32_t* rgba, cudaStream_t st);
+
 // xyz of src[0, n) into dst as 3 n contiguous floats, so that a read-back is one
 // contiguous copy instead of a copy of 12-byte rows out of 16-byte ones.
 // Cell start/end of the sorted keys plus ps / x0s (positions in sorted-slot order).

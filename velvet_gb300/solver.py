@@ -33,6 +33,42 @@ def stream_handle(stream) -> C.c_void_p | None:
     return C.c_void_p(int(h)) if h else None
 
 
+def render_params(width: int, height: int, eye: Sequence[float], target: Sequence[float],
+                  particle_radius: float, up: Sequence[float] = (0.0, 1.0, 0.0), fov_y_deg: float = 45.0,
+                  z_near: float = 0.01, z_far: float = 100.0, light_dir: Sequence[float] = (0.3, 0.9, 0.3),
+                  tint: Sequence[float] = (0.2, 0.3, 0.6), ambient: float = 0.3,
+                  background: int = 0xFF262626) -> _abi.VtRenderParams:
+    """vt_render_params for a perspective camera at `eye` looking at `target` (the
+    matrices built by vt_camera_look_at / vt_camera_perspective)."""
+    rp = _abi.VtRenderParams()
+    rp.width, rp.height = width, height
+    f3 = lambda v: (C.c_float * 3)(*[float(a) for a in v])  # noqa: E731
+    check(lib().vt_camera_look_at(f3(eye), f3(target), f3(up), rp.view), "vt_camera_look_at")
+    check(lib().vt_camera_perspective(float(np.radians(fov_y_deg)), width / height, z_near, z_far, rp.projection),
+          "vt_camera_perspective")
+    rp.z_near = z_near
+    rp.particle_radius = particle_radius
+    L = np.asarray(light_dir, np.float64)
+    rp.light_dir[:] = [float(v) for v in (L / np.linalg.norm(L)).astype(np.float32)]
+    rp.tint[:] = [float(v) for v in tint]
+    rp.ambient = ambient
+    rp.background = background
+    return rp
+
+
+def rgba_to_rgb(img: np.ndarray) -> np.ndarray:
+    """(H, W) RGBA8 words (red in the low byte) -> (H, W, 3) uint8."""
+    return np.ascontiguousarray(img, np.uint32).view(np.uint8).reshape(img.shape + (4,))[..., :3]
+
+
+def write_ppm(path, img: np.ndarray) -> None:
+    """Writes an RGBA8 image as binary PPM (P6)."""
+    rgb = rgba_to_rgb(img)
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (rgb.shape[1], rgb.shape[0]))
+        f.write(rgb.tobytes())
+
+
 class ClothSolver:
     """One plain solver domain (all its cloths share one hash and parameter block)."""
 
@@ -192,6 +228,12 @@ class ClothSolver:
         check(lib().vt_solver_grid_tile(self._h, C.byref(v)), "vt_solver_grid_tile")
         return v.value
 
+    def render(self, rp: _abi.VtRenderParams, stream=None) -> np.ndarray:
+        """The particles as shaded spheres (vt_solver_render): (height, width) RGBA8."""
+        out = np.empty((rp.height, rp.width), np.uint32)
+        check(lib().vt_solver_render(self._h, C.byref(rp), _ptr(out), 0, stream_handle(stream)), "vt_solver_render")
+        return out
+
     # ------------------------------------------------------------------ hash views
     def table_size(self) -> int:
         out = np.zeros(1, dtype=np.int32)
@@ -311,6 +353,12 @@ class BatchSolver:
         v = C.c_int32()
         check(lib().vt_batch_grid_tile(self._h, C.byref(v)), "vt_batch_grid_tile")
         return v.value
+
+    def render(self, rp: _abi.VtRenderParams, stream=None) -> np.ndarray:
+        """Every cloth's particles as shaded spheres (vt_batch_render): (height, width) RGBA8."""
+        out = np.empty((rp.height, rp.width), np.uint32)
+        check(lib().vt_batch_render(self._h, C.byref(rp), _ptr(out), 0, stream_handle(stream)), "vt_batch_render")
+        return out
 
 
 class ClothServer:
