@@ -92,11 +92,45 @@ def iteration_bytes(wl) -> float:
     return b
 
 
+def frame_bytes(wl, k_mean: float, interleaved_hash: int = 3) -> float:
+    """Algorithmic bytes of one frame over every cloth (compulsory traffic, vec3 = 12 B,
+    index = 4 B, each datum once per kernel phase): per substep predict 48 + SDF 36 +
+    finalize 48 + collide 40 + 4(k+1) per particle, per hash 20 + 16 ceil(bits/8) + 4 + 8
+    + 8 + 28 + 4(k+1) per particle (keys, sort passes, ranges, neighbour lists), per frame
+    pre-SDF 24 + 24 + normals 24 per particle, plus the iterations' bytes."""
+    hashes = -(-wl.substeps // interleaved_hash)  # substeps 0, I_h, 2 I_h, ...
+    b = wl.substeps * wl.iterations * iteration_bytes(wl)
+    for c in wl.cloths:
+        n = c.side * c.side
+        bits = max(1, math.ceil(math.log2(2 * n)))
+        b += wl.substeps * n * (48 + 36 + 48 + 40 + 4 * (k_mean + 1))
+        b += hashes * n * (20 + 16 * math.ceil(bits / 8) + 4 + 8 + 8 + 28 + 4 * (k_mean + 1))
+        b += n * (24 + 24 + 24)
+    return b
+
+
+def mean_cached_neighbours(solvers, max_particles: int = 400_000) -> float | None:
+    """k: entries per particle in the neighbour lists of a size-preserving sample of
+    simulated plain solvers (the same lists the batched form builds)."""
+    import velvet_gb300 as vg
+
+    total, count = 0, 0
+    step = max(1, int(math.ceil(sum(s[1].num_particles for s in solvers) / max_particles)))
+    for s, spec, _ in solvers[::step]:
+        nb = s.debug_view(vg._abi.DEBUG_NEIGHBORS).reshape(-1, spec.num_particles)
+        filled = nb != 0xFFFFFFFF
+        # entries before each column's terminator (a full list has none)
+        first_empty = np.where(filled.all(0), nb.shape[0], np.argmin(filled, axis=0))
+        total += int(first_empty.sum())
+        count += spec.num_particles
+    return total / count if count else None
+
+
 # DRAM traffic of one k_grid_iter launch per particle: ncu dram__bytes_read.sum +
-# dram__bytes_write.sum = 50.45 + 1.57 MB on a 1024x1024 cloth (1,050,625 particles,
-# two LRA slots); the kernel reads the same four float4 streams for every grid cloth, so
-# the figure scales with the particles a launch covers.
-GRID_ITER_DRAM_BYTES_PER_PARTICLE = (50.45e6 + 1.57e6) / 1050625
+# dram__bytes_write.sum = 50.57 + 3.18 MB on a 1024x1024 cloth (1,050,625 particles,
+# two LRA slots); the kernel reads the same float4 streams for every grid cloth, so the
+# figure scales with the particles a launch covers.
+GRID_ITER_DRAM_BYTES_PER_PARTICLE = (50.57e6 + 3.18e6) / 1050625
 
 
 class ClockSampler:
@@ -679,26 +713,52 @@ def main() -> None:
                     "stage_ms_per_frame": {k: round(v[1] / 2, 4) for k, v in prof.items()}}
 
     # ---- end to end through the C ABI: colliders from host memory every frame, all
-    # positions + normals read back into pinned host memory every frame
-    host_pos = torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True)
-    host_nrm = torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True)
+    # positions + normals read back into pinned host memory every frame.  Synchronous
+    # form: each step waits for its own read-back.  Pipelined form (the headline): frame
+    # k+1 is enqueued while frame k's read-back copies run on a second stream, the host
+    # waits for frame k's copies before enqueuing frame k+2, and every copy completes
+    # inside the timed region.
+    host_pos = [torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    host_nrm = [torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
     sh = vg.stream_handle(stream)
+    copy_stream = torch.cuda.Stream()
+    ch = vg.stream_handle(copy_stream)
+    copied = [torch.cuda.Event(), torch.cuda.Event()]
 
     def e2e_step(f):
         batch_frame(wl, batch, f, stream, upload_colliders=True)
-        _abi.check(vg.lib().vt_batch_all_get(batch.handle, 0, host_pos.data_ptr(), 1, sh), "all_get")
-        _abi.check(vg.lib().vt_batch_all_get(batch.handle, 1, host_nrm.data_ptr(), 1, sh), "all_get")
+        _abi.check(vg.lib().vt_batch_all_get(batch.handle, 0, host_pos[0].data_ptr(), 1, sh), "all_get")
+        _abi.check(vg.lib().vt_batch_all_get(batch.handle, 1, host_nrm[0].data_ptr(), 1, sh), "all_get")
         stream.synchronize()
 
+    def e2e_pipelined(f):
+        batch_frame(wl, batch, f, stream, upload_colliders=True)
+        _abi.check(vg.lib().vt_batch_all_get_async(batch.handle, 0, host_pos[f % 2].data_ptr(), ch), "all_get_async")
+        _abi.check(vg.lib().vt_batch_all_get_async(batch.handle, 1, host_nrm[f % 2].data_ptr(), ch), "all_get_async")
+        copied[f % 2].record(copy_stream)
+        if f > 0:
+            copied[(f - 1) % 2].synchronize()  # frame f-1 is in host memory
+
+    e2e_steps = max(3, args.steps // 2)
     for f in range(args.warmup):
         e2e_step(f)
     dist_sync()
-    e2e_steps = max(3, args.steps // 2)
     t0 = time.perf_counter()
     for k in range(e2e_steps):
         e2e_step(k)
+    e2e_sync_s = max_over_ranks(time.perf_counter() - t0)
+    for f in range(args.warmup):
+        e2e_pipelined(f)
+    copy_stream.synchronize()
+    dist_sync()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        e2e_pipelined(k)
+    copy_stream.synchronize()
+    stream.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_value = pits * e2e_steps * world / e2e_s
+    e2e_sync_value = pits * e2e_steps * world / e2e_sync_s
     ncol = sum(len(c.colliders(0)) for c in wl.cloths)
     h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
     d2h = n_tot * 24
@@ -717,6 +777,14 @@ def main() -> None:
         plain = {"value": pits * psteps * world / (p_ms / 1000.0), "unit": UNIT, "steps": psteps,
                  "ms_per_step": p_ms / psteps, "p50_frame_ms": statistics.median(p_per),
                  "p99_frame_ms": pct(p_per, 0.99), "form": "one vt_simulate per cloth per frame, CUDA graphs"}
+        k_mean = mean_cached_neighbours(solvers)
+        if roofline is not None and k_mean is not None:
+            fb = frame_bytes(wl, k_mean)
+            ach = fb / (total_ms / args.steps / 1000.0) / 1e9
+            roofline["frame"] = {"bytes_per_particle_iteration": fb / pits, "k_mean_measured": k_mean,
+                                 "bytes_per_frame": fb, "achieved": ach, "frac": ach / peak,
+                                 "model": "per-frame compulsory bytes (iterations + predict, SDF, collide, "
+                                          "finalize, hash, normals) / event-timed frame"}
         for s, _, _ in solvers:
             s.close()
 
@@ -741,7 +809,10 @@ def main() -> None:
             "plain": plain,
             "batched_over_plain": (value / plain["value"]) if plain else None,
             "clocks": clock_info,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "mode": "pipelined: frame k+1 computes while frame k's positions and normals copy to pinned "
+                            "host memory (vt_batch_all_get_async); all copies inside the timed region",
+                    "synchronous_value": e2e_sync_value},
             "gpu_launches": launches_timed,
             "roofline": roofline,
             "cpu_baseline": cpu,

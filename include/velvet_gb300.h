@@ -302,6 +302,13 @@ vt_status vt_batch_velocities_get(vt_batch* b, int32_t index, float* dst, int32_
  * 1 normals, 2 velocities. */
 vt_status vt_batch_all_get(vt_batch* b, int32_t what, float* dst, int32_t dst_on_device, void* stream);
 
+/* Pipelined read-back of every particle (what as vt_batch_all_get): packs on the
+ * stream of the last vt_batch_simulate into one of two device buffers used in turn, then
+ * copies into dst (pinned host or device memory) on copy_stream; returns at once.  The
+ * next frames may be enqueued while the copy runs; dst is complete when copy_stream has
+ * passed this call.  A buffer is reused only after its previous copy ended. */
+vt_status vt_batch_all_get_async(vt_batch* b, int32_t what, float* dst, void* copy_stream);
+
 /* Kernels enqueued by this batch so far (graph replays count their kernel nodes). */
 vt_status vt_batch_launch_count(const vt_batch* b, uint64_t* out);
 

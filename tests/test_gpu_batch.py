@@ -88,3 +88,38 @@ def test_batch_launch_count_is_per_frame_not_per_cloth():
     # the first frame also times the grid tile shapes (a few extra launches, once)
     assert per_frame == counts[1] - counts[0] and counts[0] >= per_frame
     assert per_frame < 40 + 3 * wl.substeps * wl.iterations
+
+
+def test_pipelined_read_back_returns_every_frame():
+    """vt_batch_all_get_async: frame k's positions copy on a second stream while frame
+    k+1 is enqueued; each frame's copy holds exactly that frame's state."""
+    import torch
+
+    wl = mixed(4, seed=5)
+
+    def build():
+        b = vg.BatchSolver()
+        for spec in wl.cloths:
+            s = vg.ClothSolver()
+            W.build_plain(spec, s)
+            b.add(s)
+        return b
+
+    ref, b = build(), build()
+    frames = 5
+    want = []
+    for _ in range(frames):
+        ref.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin)
+        ref.sync()
+        want.append(ref.all_positions())
+    n = sum(b.sizes)
+    hosts = [torch.empty((n, 3), dtype=torch.float32, pin_memory=True) for _ in range(frames)]
+    compute, copy = torch.cuda.Stream(), torch.cuda.Stream()
+    for f in range(frames):
+        b.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin,
+                   stream=compute)
+        assert vg.lib().vt_batch_all_get_async(b.handle, 0, hosts[f].data_ptr(), vg.stream_handle(copy)) == 0
+    copy.synchronize()
+    compute.synchronize()
+    for f in range(frames):
+        assert np.array_equal(bits(hosts[f].numpy()), bits(want[f])), f"frame {f}"

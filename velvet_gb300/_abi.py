@@ -194,6 +194,7 @@ SIGNATURES: dict[str, tuple] = {
     "vt_batch_normals_get": (I32, [P, I32, P, I32, P]),
     "vt_batch_velocities_get": (I32, [P, I32, P, I32, P]),
     "vt_batch_all_get": (I32, [P, I32, P, I32, P]),
+    "vt_batch_all_get_async": (I32, [P, I32, P, P]),
     "vt_batch_launch_count": (I32, [P, C.POINTER(C.c_uint64)]),
     "vt_batch_use_graphs": (I32, [P, I32]),
     "vt_server_create": (I32, [C.POINTER(VtServerConfig), C.POINTER(P)]),

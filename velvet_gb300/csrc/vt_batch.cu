@@ -16,6 +16,21 @@ struct vt_batch {
     bool use_graph = true;
     cudaStream_t stream = nullptr;
     uint64_t launches_before = 0;
+    // pipelined read-back (vt_batch_all_get_async): two packed buffers used in turn, each
+    // with an event after its pack (compute stream) and after its copy (copy stream)
+    float* rb_buf[2] = {nullptr, nullptr};
+    size_t rb_floats = 0;
+    cudaEvent_t rb_packed[2] = {nullptr, nullptr}, rb_copied[2] = {nullptr, nullptr};
+    int rb_next = 0;
+
+    ~vt_batch()
+    {
+        for (int k = 0; k < 2; ++k) {
+            if (rb_buf[k]) cudaFree(rb_buf[k]);
+            if (rb_packed[k]) cudaEventDestroy(rb_packed[k]);
+            if (rb_copied[k]) cudaEventDestroy(rb_copied[k]);
+        }
+    }
 };
 
 #define VT_CHECK(cond, code, msg) \
@@ -253,6 +268,43 @@ vt_status vt_batch_all_get(vt_batch* b, int32_t what, float* dst, int32_t on_dev
                                 st),
                 "copy out");
     if (!on_dev) VT_TRY_CUDA(cudaStreamSynchronize(st), "sync");
+    return VT_OK;
+}
+
+vt_status vt_batch_all_get_async(vt_batch* b, int32_t what, float* dst, void* copy_stream)
+{
+    VT_CHECK(b && dst, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    VT_CHECK(what >= 0 && what <= 2, VT_ERR_INVALID_ARGUMENT, "what must be 0, 1 or 2");
+    VT_CHECK(b->world.built() && !b->dirty, VT_ERR_STATE, "state exists on the device after the first simulate");
+    const size_t n = (size_t)b->world.n_particles;
+    if (!n) return VT_OK;
+    if (b->rb_floats < 3 * n) {
+        for (int k = 0; k < 2; ++k) {
+            if (b->rb_buf[k]) VT_TRY_CUDA(cudaFree(b->rb_buf[k]), "cudaFree(read-back)");
+            b->rb_buf[k] = nullptr;
+        }
+        b->rb_floats = 0;
+        for (int k = 0; k < 2; ++k) {
+            VT_TRY_CUDA(cudaMalloc(&b->rb_buf[k], 12 * n), "cudaMalloc(read-back)");
+            if (!b->rb_packed[k])
+                VT_TRY_CUDA(cudaEventCreateWithFlags(&b->rb_packed[k], cudaEventDisableTiming), "event");
+            if (!b->rb_copied[k])
+                VT_TRY_CUDA(cudaEventCreateWithFlags(&b->rb_copied[k], cudaEventDisableTiming), "event");
+        }
+        b->rb_floats = 3 * n;
+    }
+    const int k = b->rb_next;
+    b->rb_next ^= 1;
+    const float4* src = what == 0 ? b->world.d.x : what == 1 ? b->world.d.nrm : b->world.d.v;
+    cudaStream_t cs = b->stream, xs = (cudaStream_t)copy_stream;
+    // the buffer's previous copy has left it; the pack sees every frame enqueued so far
+    VT_TRY_CUDA(cudaStreamWaitEvent(cs, b->rb_copied[k], 0), "wait copy");
+    VT_TRY_CUDA(vt::launch_pack_xyz(src, b->rb_buf[k], (int64_t)n, cs), "pack");
+    b->world.launches += 1;
+    VT_TRY_CUDA(cudaEventRecord(b->rb_packed[k], cs), "event");
+    VT_TRY_CUDA(cudaStreamWaitEvent(xs, b->rb_packed[k], 0), "wait pack");
+    VT_TRY_CUDA(cudaMemcpyAsync(dst, b->rb_buf[k], 12 * n, cudaMemcpyDefault, xs), "copy out");
+    VT_TRY_CUDA(cudaEventRecord(b->rb_copied[k], xs), "event");
     return VT_OK;
 }
 
