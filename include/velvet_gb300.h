@@ -255,6 +255,17 @@ vt_status vt_solver_launch_count(const vt_solver* s, uint64_t* out);
  * directly, as the reference does. */
 vt_status vt_solver_use_graphs(vt_solver* s, int32_t on);
 
+/* ------------------------------------------------------------------ checkpoint / resume
+ * The simulation state of a solver as one flat binary (no reference counterpart; a reset
+ * there re-runs the scene): a 16-byte header (magic "VTCK", version 1, particle count,
+ * slot count), then positions (3 floats each), velocities (3), inverse masses (1) and
+ * attach slot positions (3).  Loading it into a solver registered the same way (same
+ * particle and slot counts) and continuing gives the bits the saved solver would have
+ * produced: everything else a frame reads is rebuilt from these. */
+vt_status vt_solver_state_size(const vt_solver* s, uint64_t* bytes);
+vt_status vt_solver_state_save(vt_solver* s, void* dst, uint64_t bytes);
+vt_status vt_solver_state_load(vt_solver* s, const void* src, uint64_t bytes);
+
 /* ------------------------------------------------------------------ batched solver
  * Many independent cloths advanced together.  Each cloth is registered on its own
  * vt_solver (the plain API above), then copied into the batch, where it keeps its own
@@ -340,6 +351,7 @@ typedef struct vt_server_config {
 #define VT_REQ_QUEUED 0
 #define VT_REQ_ACTIVE 1
 #define VT_REQ_DONE   2
+#define VT_REQ_FAILED 3  /* its state became NaN / Inf: evicted, no result (VT_ERR_NUMERIC) */
 
 typedef struct vt_server_tick_info {
     int32_t  admitted, retired, active, queued;
@@ -354,6 +366,7 @@ typedef struct vt_server_stats {
     double   gpu_ms;               /* sum of frame_ms                                        */
     double   p50_frame_ms, p99_frame_ms;  /* over all (request, frame) pairs                 */
     uint64_t bytes_in_use, bytes_budget;
+    uint64_t requests_failed;      /* evicted after a NaN / Inf fault, the others unaffected */
 } vt_server_stats;
 
 vt_status vt_server_create(const vt_server_config* cfg, vt_server** out);
@@ -393,9 +406,13 @@ vt_status vt_server_submit_grid(vt_server* s, const vt_grid_cloth* cloth, const 
  * the old one first). */
 vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info);
 
+/* State (VT_REQ_*) and frames completed.  A request whose state turns NaN / Inf raises
+ * its slot's fault flag; the tick that sees the flag evicts it at the next tick
+ * (VT_REQ_FAILED, counted in requests_failed) and no other request is affected. */
 vt_status vt_server_poll(vt_server* s, int64_t request_id, int32_t* state, int32_t* frames_done);
 
-/* Final positions of a finished request (count = its particle count) into host memory. */
+/* Final positions of a finished request (count = its particle count) into host memory;
+ * VT_ERR_NUMERIC for an evicted request. */
 vt_status vt_server_result(vt_server* s, int64_t request_id, float* dst, uint32_t count);
 
 vt_status vt_server_stats_get(vt_server* s, vt_server_stats* out);

@@ -155,6 +155,40 @@ def test_described_grid_cloth_arguments_are_checked():
     assert e.value.status == _abi.VT_ERR_CAPACITY  # larger than the arena
 
 
+def test_a_request_that_turns_nan_is_evicted_and_the_others_are_untouched():
+    """Failure isolation: a request seeded with a NaN velocity raises its slot's fault flag
+    in its first frame; the server evicts it (VT_REQ_FAILED, no result) and every other
+    request of the mix still ends with its bits when simulated alone."""
+    srv = vg.ClothServer(hbm_budget_bytes=1 << 30, max_cloths=8, substeps=3, iterations=4)
+    good = [(request(20, 0.5), 6), (request(27, 0.55), 5)]
+    ids = []
+    for k, (spec, frames) in enumerate(good):
+        s = registered(spec)
+        ids.append((srv.submit(s, frames), spec, frames))
+        s.close()
+        if k == 0:  # the faulty one arrives between the two good ones
+            bad = registered(request(16, 0.45))
+            v = bad.velocities()
+            v[7] = np.nan
+            bad.set_velocities(v)
+            bad_id = srv.submit(bad, 8)
+            bad.close()
+    for _ in range(60):
+        info = srv.tick()
+        if info.active == 0 and info.queued == 0:
+            break
+    st, done = srv.poll(bad_id)
+    assert st == _abi.REQ_FAILED and done < 8
+    with pytest.raises(vg.VtError) as e:
+        srv.result(bad_id)
+    assert e.value.status == _abi.VT_ERR_NUMERIC
+    for rid, spec, frames in ids:
+        assert srv.poll(rid) == (_abi.REQ_DONE, frames)
+        assert np.array_equal(bits(srv.result(rid)), bits(alone(spec, frames)))
+    stats = srv.stats()
+    assert stats.requests_failed == 1 and stats.requests_done == 2
+
+
 def test_rejects_non_grid_and_oversize():
     srv = vg.ClothServer(hbm_budget_bytes=1 << 27, max_cloths=2)  # ~300k particles of arena
     s = vg.ClothSolver()

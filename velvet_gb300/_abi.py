@@ -100,7 +100,7 @@ class VtServerStats(C.Structure):
         ("ticks", C.c_uint64), ("frames_done", C.c_uint64), ("requests_done", C.c_uint64),
         ("particle_iterations", C.c_double), ("gpu_ms", C.c_double),
         ("p50_frame_ms", C.c_double), ("p99_frame_ms", C.c_double),
-        ("bytes_in_use", C.c_uint64), ("bytes_budget", C.c_uint64),
+        ("bytes_in_use", C.c_uint64), ("bytes_budget", C.c_uint64), ("requests_failed", C.c_uint64),
     ]
 
 
@@ -129,7 +129,7 @@ class VtRenderParams(C.Structure):
     ]
 
 
-REQ_QUEUED, REQ_ACTIVE, REQ_DONE = 0, 1, 2
+REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 
 class VtHashParams(C.Structure):
@@ -181,6 +181,9 @@ SIGNATURES: dict[str, tuple] = {
     "vt_attach_slot_set": (I32, [P, I32, P]),
     "vt_solver_debug_get": (I32, [P, I32, P, U64]),
     "vt_solver_launch_count": (I32, [P, C.POINTER(C.c_uint64)]),
+    "vt_solver_state_size": (I32, [P, C.POINTER(C.c_uint64)]),
+    "vt_solver_state_save": (I32, [P, P, U64]),
+    "vt_solver_state_load": (I32, [P, P, U64]),
     "vt_solver_use_graphs": (I32, [P, I32]),
     "vt_batch_create": (I32, [C.POINTER(P)]),
     "vt_batch_destroy": (I32, [P]),

@@ -702,6 +702,61 @@ vt_status vt_attach_slot_set(vt_solver* s, int32_t slot, const float xyz[3])
     return VT_OK;
 }
 
+// ------------------------------------------------------------------ checkpoint / resume
+namespace {
+struct StateHeader {
+    uint32_t magic, version, n, nslots;
+};
+constexpr uint32_t kStateMagic = 0x4b435456u;  // "VTCK"
+uint64_t state_bytes(uint64_t n, uint64_t ns) { return sizeof(StateHeader) + 4 * (7 * n + 3 * ns); }
+}  // namespace
+
+vt_status vt_solver_state_size(const vt_solver* s, uint64_t* bytes)
+{
+    VT_CHECK(s && bytes, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *bytes = state_bytes(s->h.n(), s->h.nslots());
+    return VT_OK;
+}
+
+vt_status vt_solver_state_save(vt_solver* s, void* dst, uint64_t bytes)
+{
+    VT_CHECK(s && dst, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    const uint32_t n = s->h.n(), ns = s->h.nslots();
+    VT_CHECK(bytes >= state_bytes(n, ns), VT_ERR_INVALID_ARGUMENT, "buffer smaller than vt_solver_state_size");
+    VT_GUARD_BEGIN
+    const StateHeader hd{kStateMagic, 1u, n, ns};
+    std::memcpy(dst, &hd, sizeof(hd));
+    float* f = reinterpret_cast<float*>(static_cast<char*>(dst) + sizeof(hd));
+    vt_status st = vt_positions_get(s, 0, n, f, 0, s->stream);
+    if (st == VT_OK) st = vt_velocities_get(s, 0, n, f + 3 * (size_t)n, 0, s->stream);
+    if (st == VT_OK) st = vt_inv_mass_get(s, 0, n, f + 6 * (size_t)n);
+    if (st != VT_OK) return st;
+    if (ns) std::memcpy(f + 7 * (size_t)n, s->h.slots.data(), 12 * (size_t)ns);
+    return VT_OK;
+    VT_GUARD_END
+}
+
+vt_status vt_solver_state_load(vt_solver* s, const void* src, uint64_t bytes)
+{
+    VT_CHECK(s && src, VT_ERR_INVALID_ARGUMENT, "NULL argument");
+    VT_CHECK(bytes >= sizeof(StateHeader), VT_ERR_INVALID_ARGUMENT, "buffer too small");
+    StateHeader hd;
+    std::memcpy(&hd, src, sizeof(hd));
+    VT_CHECK(hd.magic == kStateMagic && hd.version == 1, VT_ERR_INVALID_ARGUMENT, "not a solver state");
+    VT_CHECK(hd.n == s->h.n() && hd.nslots == s->h.nslots(), VT_ERR_INVALID_ARGUMENT,
+             "state of a solver with other particle or slot counts");
+    VT_CHECK(bytes >= state_bytes(hd.n, hd.nslots), VT_ERR_INVALID_ARGUMENT, "truncated state");
+    VT_GUARD_BEGIN
+    const float* f = reinterpret_cast<const float*>(static_cast<const char*>(src) + sizeof(hd));
+    const uint32_t n = hd.n;
+    vt_status st = vt_positions_set(s, 0, n, f, 0, s->stream);
+    if (st == VT_OK) st = vt_velocities_set(s, 0, n, f + 3 * (size_t)n, 0, s->stream);
+    if (st == VT_OK) st = vt_inv_mass_set(s, 0, n, f + 6 * (size_t)n);
+    for (uint32_t k = 0; st == VT_OK && k < hd.nslots; ++k) st = vt_attach_slot_set(s, (int32_t)k, f + 7 * (size_t)n + 3 * k);
+    return st;
+    VT_GUARD_END
+}
+
 vt_status vt_solver_debug_get(vt_solver* s, int32_t what, void* dst, uint64_t bytes)
 {
     VT_CHECK(s && dst, VT_ERR_INVALID_ARGUMENT, "NULL argument");

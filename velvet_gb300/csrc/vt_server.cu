@@ -52,6 +52,7 @@ struct Request {
     uint32_t n = 0;
     const float* res_pin = nullptr;  // result in a pinned ring (copied out when complete)
     std::vector<float> result;
+    bool failed = false;  // a frame produced NaN / Inf state: evicted, reported, no result
     // described grid cloth (vt_server_submit_grid): built on the device at admission,
     // h holds its parameters, slots and colliders but no particle arrays
     bool described = false;
@@ -142,7 +143,8 @@ struct vt_server {
     cudaEvent_t staged = nullptr;
     cudaEvent_t ev0[2] = {nullptr, nullptr}, ev1[2] = {nullptr, nullptr};  // frame of tick parity
     PinnedRing up[2], res[2];
-    std::vector<Request*> members[2];    // requests in the frame of tick parity k
+    std::vector<std::pair<Request*, int32_t>> members[2];  // (request, slot) in the frame of parity k
+    int32_t* status_pin[2] = {nullptr, nullptr};  // per-slot fault flags read after each frame
     std::vector<Request*> finishing[2];  // result copies enqueued in the tick of parity k
     uint64_t frame_particles[2] = {0, 0};
     bool inflight[2] = {false, false};
@@ -176,6 +178,7 @@ struct vt_server {
             if (ev0[k]) cudaEventDestroy(ev0[k]);
             if (ev1[k]) cudaEventDestroy(ev1[k]);
             if (up[k].base) cudaFreeHost(up[k].base);
+            if (status_pin[k]) cudaFreeHost(status_pin[k]);
             if (res[k].base) cudaFreeHost(res[k].base);
         }
     }
@@ -461,6 +464,7 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
         VT_TRY_CUDA(cudaEventCreate(&s->ev1[k]), "event");
         VT_TRY_CUDA(cudaMallocHost((void**)&s->up[k].base, kUploadRingBytes), "cudaMallocHost(upload ring)");
         s->up[k].cap = kUploadRingBytes;
+        VT_TRY_CUDA(cudaMallocHost((void**)&s->status_pin[k], 4 * (M + 1)), "cudaMallocHost(fault flags)");
         VT_TRY_CUDA(cudaMallocHost((void**)&s->res[k].base, kResultRingBytes), "cudaMallocHost(result ring)");
         s->res[k].cap = kResultRingBytes;
     }
@@ -597,7 +601,25 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
     // that frame on the stream, so their range and slot are free for this tick's admissions
     for (int32_t sid = 0; sid < (int32_t)s->slot.size(); ++sid) {
         Request* r = s->slot[sid];
-        if (!r || r->enq < r->frames) continue;
+        if (!r || (r->enq < r->frames && !r->failed)) continue;
+        // the slot's fault flag is cleared before a new request can take the slot
+        VT_TRY_CUDA(cudaMemsetAsync(s->d.status + 1 + sid, 0, 4, st), "clear fault flag");
+        if (r->failed) {  // evicted: no result, the range and slot return at once
+            k_fill_i32<<<(unsigned)((r->n + 255) / 256), 256, 0, st>>>(s->pdom + r->pb, (int64_t)r->n, -1);
+            VT_TRY_CUDA(cudaGetLastError(), "clear domain ids");
+            s->launches += 1;
+            s->alloc.release(r->pb, r->n);
+            s->active_particles -= r->n;
+            s->n_active -= 1;
+            s->slot[sid] = nullptr;
+            r->sid = -1;
+            r->state = VT_REQ_FAILED;
+            r->h = vt::HostSolver{};
+            s->stats.requests_failed += 1;
+            s->tables_dirty = true;
+            ti.retired += 1;
+            continue;
+        }
         float* pk = s->d.packed + 3 * r->pb;
         VT_TRY_CUDA(vt::launch_pack_xyz(s->d.x + r->pb, pk, (int64_t)r->n, st), "pack result");
         s->launches += 1;
@@ -664,11 +686,14 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
         VT_TRY_CUDA(cudaEventRecord(s->ev0[par], st), "event");
         const vt_status fr = run_frame(s, st);
         if (fr != VT_OK) return fr;
+        VT_TRY_CUDA(cudaMemcpyAsync(s->status_pin[par], s->d.status, 4 * (s->slot.size() + 1),
+                                    cudaMemcpyDeviceToHost, st),
+                    "read fault flags");
         VT_TRY_CUDA(cudaEventRecord(s->ev1[par], st), "event");
-        for (Request* r : s->slot)
-            if (r) {
+        for (int32_t sid = 0; sid < (int32_t)s->slot.size(); ++sid)
+            if (Request* r = s->slot[sid]) {
                 r->enq += 1;
-                s->members[par].push_back(r);
+                s->members[par].push_back({r, sid});
             }
         s->frame_particles[par] = s->active_particles;
         s->inflight[par] = true;
@@ -679,7 +704,10 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
         float ms = 0;
         VT_TRY_CUDA(cudaEventElapsedTime(&ms, s->ev0[prev], s->ev1[prev]), "elapsed");
         ti.frame_ms = ms;
-        for (Request* r : s->members[prev]) r->done += 1;
+        for (const auto& m : s->members[prev]) {
+            m.first->done += 1;
+            if (s->status_pin[prev][1 + m.second] != 0) m.first->failed = true;  // evicted next tick
+        }
         const int32_t m = (int32_t)s->members[prev].size();
         s->frame_log.emplace_back(ms, m);
         s->stats.ticks += 1;
@@ -692,11 +720,14 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
         VT_TRY_CUDA(cudaStreamSynchronize(st), "result copies");
     }
     for (Request* r : s->finishing[prev]) {
-        if (r->res_pin) r->result.assign(r->res_pin, r->res_pin + 3 * (size_t)r->n);
+        if (r->res_pin && !r->failed) r->result.assign(r->res_pin, r->res_pin + 3 * (size_t)r->n);
         r->res_pin = nullptr;
-        r->state = VT_REQ_DONE;
+        r->state = r->failed ? VT_REQ_FAILED : VT_REQ_DONE;  // a fault in the last frame
         r->h = vt::HostSolver{};  // release the staging copy
-        s->stats.requests_done += 1;
+        if (r->failed)
+            s->stats.requests_failed += 1;
+        else
+            s->stats.requests_done += 1;
         s->n_finishing -= 1;
     }
     s->finishing[prev].clear();
@@ -727,6 +758,7 @@ vt_status vt_server_result(vt_server* s, int64_t id, float* dst, uint32_t count)
     auto it = s->reqs.find(id);
     VT_CHECK(it != s->reqs.end(), VT_ERR_NOT_FOUND, "unknown request");
     const Request& r = *it->second;
+    VT_CHECK(r.state != VT_REQ_FAILED, VT_ERR_NUMERIC, "the request's state became NaN / Inf; it was evicted");
     VT_CHECK(r.state == VT_REQ_DONE, VT_ERR_STATE, "request not finished");
     VT_CHECK(count == r.n, VT_ERR_INVALID_ARGUMENT, "count must equal the request's particle count");
     std::memcpy(dst, r.result.data(), 12 * (size_t)count);

@@ -228,6 +228,19 @@ class ClothSolver:
         check(lib().vt_solver_grid_tile(self._h, C.byref(v)), "vt_solver_grid_tile")
         return v.value
 
+    def save_state(self) -> bytes:
+        """Checkpoint (vt_solver_state_save): positions, velocities, inverse masses, slots."""
+        n = C.c_uint64()
+        check(lib().vt_solver_state_size(self._h, C.byref(n)), "vt_solver_state_size")
+        buf = (C.c_char * n.value)()
+        check(lib().vt_solver_state_save(self._h, buf, n.value), "vt_solver_state_save")
+        return bytes(buf)
+
+    def load_state(self, state: bytes) -> None:
+        """Resume from save_state() of a solver registered the same way."""
+        buf = C.create_string_buffer(state, len(state))
+        check(lib().vt_solver_state_load(self._h, buf, len(state)), "vt_solver_state_load")
+
     def render(self, rp: _abi.VtRenderParams, stream=None) -> np.ndarray:
         """The particles as shaded spheres (vt_solver_render): (height, width) RGBA8."""
         out = np.empty((rp.height, rp.width), np.uint32)
