@@ -658,10 +658,17 @@ def main() -> None:
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    def sum_over_ranks(x: float) -> float:
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
     # weak scaling: every rank simulates its own mix of cloths (seed + rank)
     wl = workload(args.workload, args.seed + rank)
     stream = torch.cuda.Stream()
     pits = pits_per_frame(wl)
+    job_pits = sum_over_ranks(pits)  # every rank's cloths differ (seed + rank)
     n_tot = wl.num_particles
     props = torch.cuda.get_device_properties(local)
     bus = getattr(props, "pci_bus_id", None)
@@ -681,7 +688,7 @@ def main() -> None:
     clock_info = clocks.stop()
     launches_timed = batch.launch_count() - l0
     total_ms = max_over_ranks(total_ms)
-    value = pits * args.steps * world / (total_ms / 1000.0)
+    value = job_pits * args.steps / (total_ms / 1000.0)
 
     # ---- roofline of the dominant stage: one Jacobi iteration (bend + solve), events
     # around each launch on the launching stream (graphs off while profiling)
@@ -757,8 +764,8 @@ def main() -> None:
     copy_stream.synchronize()
     stream.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_value = pits * e2e_steps * world / e2e_s
-    e2e_sync_value = pits * e2e_steps * world / e2e_sync_s
+    e2e_value = job_pits * e2e_steps / e2e_s
+    e2e_sync_value = job_pits * e2e_steps / e2e_sync_s
     ncol = sum(len(c.colliders(0)) for c in wl.cloths)
     h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
     d2h = n_tot * 24
@@ -774,7 +781,7 @@ def main() -> None:
         psteps = max(3, args.steps // 4)
         p_ms, p_per = timed_device(pstep, psteps, args.warmup, stream, dist_sync)
         p_ms = max_over_ranks(p_ms)
-        plain = {"value": pits * psteps * world / (p_ms / 1000.0), "unit": UNIT, "steps": psteps,
+        plain = {"value": job_pits * psteps / (p_ms / 1000.0), "unit": UNIT, "steps": psteps,
                  "ms_per_step": p_ms / psteps, "p50_frame_ms": statistics.median(p_per),
                  "p99_frame_ms": pct(p_per, 0.99), "form": "one vt_simulate per cloth per frame, CUDA graphs"}
         k_mean = mean_cached_neighbours(solvers)

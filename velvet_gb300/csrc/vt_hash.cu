@@ -17,7 +17,10 @@
 //           cells that hash to the same bucket are visited twice, as in the reference.
 // In the multi-domain form each domain hashes into its own bucket range
 // [table_base, table_base + T) so one sort serves all domains and each domain's order
-// equals the order it would have alone.
+// equals the order it would have alone.  The solver's walk runs one thread per sorted
+// slot over copies of the positions in sorted order (made with the cell ranges), so a
+// warp's threads share buckets and each candidate is one contiguous 16-byte load; the
+// caller-buffer form (HashObjects) walks the caller's float3 arrays directly.
 #include "vt_math.cuh"
 #include "vt_world.h"
 

@@ -2,6 +2,7 @@
 // one or more of them.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -58,6 +59,15 @@ struct HostSolver {
     uint32_t nslots() const { return (uint32_t)(slots.size() / 3); }
     // bytes of device memory World::build uses for this solver as one domain
     uint64_t device_bytes() const;
+};
+
+// An NVTX range over a host scope (frame submission, server tick, stage launches):
+// visible in a timeline tool when one is attached, a no-op otherwise (header-only NVTX).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 // Per-stage GPU timing (vt_profiler_*): event pairs around stage launches.

@@ -2,14 +2,16 @@
 //
 // Same arithmetic as the reference kernels (Velvet/VtClothSolverGPU.cu), different
 // packaging:
-//   * Jacobi sums are gathers, not atomics.  Each particle walks its constraints in
-//     constraint order (CSR built at registration) and adds their corrections in that
-//     order, so the sum is the one a sequential run of the reference kernels produces
-//     and is identical from run to run.  Stretch and attachment corrections are
-//     recomputed by each endpoint (the two endpoints of a stretch constraint get exact
-//     negatives of each other's intermediate values, so the recomputation is exact);
-//     bending is evaluated once per constraint into per-corner slots that the particle
-//     gather reads.
+//   * Jacobi sums are gathers, not atomics.  Each particle adds its constraints'
+//     corrections in constraint order, so the sum is the one a sequential run of the
+//     reference kernels produces and is identical from run to run.  Grid cloths (the
+//     grid builder's topology) use k_grid_iter: implicit topology, a tile of predicted
+//     positions in shared memory, every stretch and bending constraint evaluated once
+//     per tile.  Other meshes use k_bend + k_solve over CSR lists built at registration:
+//     stretch and attachment corrections recomputed by each endpoint (the two endpoints
+//     of a stretch constraint get exact negatives of each other's intermediate values,
+//     so the recomputation is exact), bending evaluated once per constraint into
+//     per-corner slots that the particle gather reads.
 //   * ApplyDeltas is fused into the gather that produces the deltas; predicted
 //     positions ping-pong between two buffers so every constraint of an iteration sees
 //     the positions of the previous iteration, as the reference's launch order implies.
@@ -17,6 +19,7 @@
 //     substep's PredictPositions are fused into the last iteration's gather; the
 //     pre-stabilisation CollideSDF is fused with the first PredictPositions.
 //   * float4 particles (w = inverse mass) so each particle is one 16-byte load.
+// Also here: the device grid builder (k_grid_build) and read-back packing (k_pack_xyz).
 #include "vt_math.cuh"
 #include "vt_world.h"
 

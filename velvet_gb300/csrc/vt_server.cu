@@ -591,6 +591,7 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
     VT_CHECK(s, VT_ERR_INVALID_ARGUMENT, "NULL server");
     VT_GUARD_BEGIN
     cudaStream_t st = (cudaStream_t)stream;
+    vt::NvtxRange range("vt server tick");
     if (s->stream_set && st != s->last_stream)  // the pipeline is ordered by one stream
         VT_TRY_CUDA(cudaStreamSynchronize(s->last_stream), "previous stream");
     s->last_stream = st;

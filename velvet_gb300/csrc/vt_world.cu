@@ -1,16 +1,18 @@
-// vt_world.cu — builds the device state of one or more solver domains (CSR adjacency,
-// tile tables, hash buffers) and enqueues the launches of one frame.
+// vt_world.cu — builds the device state of one or more solver domains (grid rests and
+// tiles for grid cloths, CSR adjacency for other meshes, hash buffers), autotunes the
+// grid kernel's tile variant, and enqueues (or replays as a CUDA graph) one frame.
 //
 // Schedule of one frame (Velvet/VtClothSolverGPU.hpp:56-111, with the fusions listed
 // in vt_kernels.cu):
 //   presdf_predict                           CollideSDF(x, frameDt) + Predict(substep 0)
 //   for each substep s:
 //     if self-collision and s % interleavedHash == 0:
-//        fill cell_start 0xff, hash_keys, radix sort, cell_ranges, cache_neighbors
+//        fill cell_start 0xff, hash_keys, radix sort, cell_ranges_gather
+//        (+ sorted copies of the positions), cache_neighbors
 //     collide                                CollideParticles + ApplyDeltas + CollideSDF
-//     for each iteration: bend, solve        Stretch + Attach + Bending + ApplyDeltas
-//       (the last iteration's solve also runs Finalize and, except after the last
-//        substep, the next substep's Predict)
+//     for each iteration:                    Stretch + Attach + Bending + ApplyDeltas
+//       grid_iter (grid domains) and bend + solve (CSR domains); the last iteration
+//       also runs Finalize and, except after the last substep, the next Predict
 //   normals
 #include <algorithm>
 #include <cstring>
@@ -105,6 +107,7 @@ bool profiler_on() { return prof().on; }
 
 StageScope::StageScope(int stage_, cudaStream_t st_) : stage(stage_), st(st_)
 {
+    nvtxRangePushA(stage_name(stage_));
     ProfilerState& P = prof();
     if (!P.on) return;
     std::lock_guard<std::mutex> lock(P.mu);
@@ -115,6 +118,7 @@ StageScope::StageScope(int stage_, cudaStream_t st_) : stage(stage_), st(st_)
 
 StageScope::~StageScope()
 {
+    nvtxRangePop();
     if (!e0) return;
     ProfilerState& P = prof();
     std::lock_guard<std::mutex> lock(P.mu);
@@ -740,6 +744,7 @@ vt_status World::simulate(const FrameArgs& a, int32_t ih, bool any_self, cudaStr
 {
     if (!built_) return VT_ERR_STATE;
     if (n_particles == 0) return VT_OK;
+    NvtxRange range("vt frame");
     vt_status r = upload_frame(st);
     if (r != VT_OK) return r;
     if (!tuned_) {
