@@ -31,6 +31,15 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
+def test_bounds_checked_build_exports_the_same_symbols():
+    """build() also makes the bounds-checked library from the same sources."""
+    path = Path(_abi.__file__).resolve().parent / "libvelvet_gb300_checked.so"
+    assert path.exists(), "run __graft_entry__.build() first"
+    L = C.CDLL(str(path))
+    missing = [f for f in declared_functions() if not hasattr(L, f)]
+    assert not missing, missing
+
+
 def test_abi_version():
     assert vg.lib().vt_abi_version() == 1
 

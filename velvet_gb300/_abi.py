@@ -1,15 +1,19 @@
 """ctypes view of include/velvet_gb300.h.
 
-`lib()` loads velvet_gb300/libvelvet_gb300.so (built in-tree by velvet_gb300.build)
+`lib()` loads velvet_gb300/libvelvet_gb300.so (built in-tree by velvet_gb300.build; with
+VT_CHECKED=1 in the environment, its bounds-checked build libvelvet_gb300_checked.so)
 and declares every entry point's signature.  There is no fallback: if the library is
 missing or fails to load, `lib()` raises.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libvelvet_gb300.so"
+# VT_CHECKED=1 loads the bounds-checked build of the same sources (see build.py)
+LIB_PATH = Path(__file__).resolve().parent / (
+    "libvelvet_gb300_checked.so" if os.environ.get("VT_CHECKED") == "1" else "libvelvet_gb300.so")
 
 VT_OK = 0
 VT_ERR_INVALID_ARGUMENT = -1

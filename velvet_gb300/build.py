@@ -6,6 +6,10 @@ include/velvet_gb300.h.  Flags that matter for results:
   -fmad=false                 no multiply-add contraction in device code
   -Xcompiler -ffp-contract=off  the same for host code (gcc on aarch64 contracts by default)
 so every FP32 result is the IEEE-rounded value of the operations as written.
+
+build(checked=True) makes libvelvet_gb300_checked.so from the same sources with
+-DVT_CHECKED=1: data-dependent device indices are range-checked and a failure is reported
+by the sync calls (the library the tests can load instead with VT_CHECKED=1).
 """
 from __future__ import annotations
 
@@ -21,6 +25,8 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 OUT = PKG / "libvelvet_gb300.so"
 OBJ = PKG / "_build"
+OUT_CHECKED = PKG / "libvelvet_gb300_checked.so"
+OBJ_CHECKED = PKG / "_build_checked"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -36,9 +42,9 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build velvet_gb300")
 
 
-def _compile(src: Path, verbose_ptxas: bool) -> Path:
-    obj = OBJ / (src.stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+def _compile(src: Path, verbose_ptxas: bool, checked: bool = False) -> Path:
+    obj = (OBJ_CHECKED if checked else OBJ) / (src.stem + ".o")
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *(["-DVT_CHECKED=1"] if checked else []), "-c", str(src), "-o", str(obj)]
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -53,31 +59,31 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
 
 
-def up_to_date() -> bool:
-    if not OUT.exists():
+def up_to_date(out: Path = OUT) -> bool:
+    if not out.exists():
         return False
-    t = OUT.stat().st_mtime
+    t = out.stat().st_mtime
     deps = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
     return all(p.stat().st_mtime <= t for p in deps)
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
-    """Compiles and links the library if any source is newer than it."""
-    if not force and up_to_date():
-        return OUT
-    OBJ.mkdir(exist_ok=True)
+def build(force: bool = False, verbose_ptxas: bool = False, checked: bool = False) -> Path:
+    """Compiles and links the library (or its bounds-checked twin) if any source is newer."""
+    out, obj_dir = (OUT_CHECKED, OBJ_CHECKED) if checked else (OUT, OBJ)
+    if not force and up_to_date(out):
+        return out
+    obj_dir.mkdir(exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), srcs))
-    tmp = OUT.with_suffix(".so.tmp")
+        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas, checked), srcs))
+    tmp = out.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, OUT)
-    return OUT
+    os.replace(tmp, out)
+    return out
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv)
-    print(OUT)
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv, checked="--checked" in sys.argv))

@@ -214,6 +214,10 @@ vt_status vt_batch_sync(vt_batch* b)
     if (flags[0]) {
         b->world.clear_status(b->stream);
         VT_TRY_CUDA(cudaStreamSynchronize(b->stream), "sync");
+        if (flags[0] & vt::VT_STATUS_BOUNDS) {
+            vt::set_error("a device-side bounds check failed (bounds-checked build)");
+            return VT_ERR_STATE;
+        }
         vt::set_error("non-finite particle state detected on the device");
         return VT_ERR_NUMERIC;
     }

@@ -563,6 +563,10 @@ vt_status vt_solver_sync(vt_solver* s)
     if (flags[0]) {
         s->world.clear_status(s->stream);
         VT_TRY_CUDA(cudaStreamSynchronize(s->stream), "sync");
+        if (flags[0] & vt::VT_STATUS_BOUNDS) {
+            vt::set_error("a device-side bounds check failed (bounds-checked build)");
+            return VT_ERR_STATE;
+        }
         vt::set_error("non-finite particle state detected on the device");
         return VT_ERR_NUMERIC;
     }

@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kBlock)
 k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int32_t n, int shift,
                int nbits, const uint32_t* __restrict__ hist, const uint32_t* __restrict__ digit_tot,
-               int32_t ntiles)
+               int32_t ntiles, int32_t* __restrict__ status)
 {
     __shared__ uint32_t off[256];
     __shared__ uint32_t wcnt[kRsWarps][256];
@@ -212,6 +212,7 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
         if (idx < n) {
             const uint32_t d = (mk[j] >> shift) & mask;
             const uint32_t pos = off[d] + wcnt[warp][d] + mr[j];
+            if (!VT_IN_RANGE(pos, 0, n, status)) continue;
             kout[pos] = mk[j];
             vout[pos] = mv[j];
         }
@@ -220,7 +221,7 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
 
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                              uint32_t* hist, uint32_t* digit_tot, int32_t n, int32_t bits,
-                             cudaStream_t st)
+                             cudaStream_t st, int32_t* status)
 {
     if (n <= 1 || bits <= 0) return cudaSuccess;
     const int passes = (bits + 7) / 8;
@@ -232,7 +233,7 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
         const int nb = (bits - shift) < per ? (bits - shift) : per;
         k_rs_upsweep<<<ntiles, kBlock, 0, st>>>(ki, n, shift, nb, hist, ntiles);
         k_rs_scan<<<1 << nb, kBlock, 0, st>>>(hist, ntiles, digit_tot);
-        k_rs_downsweep<<<ntiles, kBlock, 0, st>>>(ki, vi, ko, vo, n, shift, nb, hist, digit_tot, ntiles);
+        k_rs_downsweep<<<ntiles, kBlock, 0, st>>>(ki, vi, ko, vo, n, shift, nb, hist, digit_tot, ntiles, status);
         uint32_t* t;
         t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
@@ -280,7 +281,7 @@ __global__ void __launch_bounds__(kBlock)
 k_cell_ranges_gather(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                      const float4* __restrict__ p, const float4* __restrict__ x0, int32_t n,
                      uint32_t* __restrict__ cs, uint32_t* __restrict__ ce, float4* __restrict__ ps,
-                     float4* __restrict__ x0s)
+                     float4* __restrict__ x0s, int32_t* __restrict__ status)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
     if (t >= n) return;
@@ -291,6 +292,7 @@ k_cell_ranges_gather(const uint32_t* __restrict__ keys, const uint32_t* __restri
     }
     if (t == n - 1) ce[h] = (uint32_t)n;
     const uint32_t id = vals[t];
+    if (!VT_IN_RANGE(id, 0, n, status)) return;
     const float4 q = p[id];
     ps[t] = make_float4(q.x, q.y, q.z, __uint_as_float(id));
     x0s[t] = x0[id];
@@ -300,7 +302,8 @@ cudaError_t launch_cell_ranges_gather(const DeviceArrays& d, int pin, int32_t n,
 {
     if (n <= 0) return cudaSuccess;
     k_cell_ranges_gather<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(d.keys, d.vals, d.p[pin], d.x0, n,
-                                                                      d.cell_start, d.cell_end, d.ps, d.x0s);
+                                                                      d.cell_start, d.cell_end, d.ps, d.x0s,
+                                                                      d.status);
     return cudaGetLastError();
 }
 
@@ -374,7 +377,7 @@ __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint32_
                                                        uint32_t* __restrict__ out_base, uint32_t id_base,
                                                        int32_t n, int32_t table_base, int32_t table,
                                                        uint64_t M, float sp, float sp2, float diam2,
-                                                       int32_t max_nbr)
+                                                       int32_t max_nbr, uint32_t slot_end, int32_t* status)
 {
     const float4 own = ps[t];
     const uint32_t id = __float_as_uint(own.w);
@@ -402,9 +405,11 @@ __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint32_
                 uint32_t end = ce[h];
                 const uint32_t lim = start + (uint32_t)max_nbr;
                 if (lim < end) end = lim;
+                if (!VT_IN_RANGE(end, start, (long long)slot_end + 1, status)) continue;
                 for (uint32_t k = start; k < end; ++k) {
                     const float4 qk = ps[k];
                     const uint32_t nb = __float_as_uint(qk.w);
+                    if (!VT_IN_RANGE(nb, id_base, id_base + (uint32_t)n, status)) continue;
                     const vec3 d1 = position - xyz(qk);
                     if (nb == id) continue;
                     if (!(dot(d1, d1) < sp2)) continue;
@@ -438,15 +443,17 @@ struct PosF3 {
 __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
                   const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
-                  const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr)
+                  const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
+                  int32_t* __restrict__ status)
 {
     const Tile tl = tiles[blockIdx.x];
     const int t = tl.begin + (int)threadIdx.x;
     if (t >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
+    // a domain's sorted slots are its particle range
     cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + D.nbr_base, (uint32_t)D.p_begin, D.p_count,
                            D.table_base, D.table_size, ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing,
-                           D.cell_spacing2, D.diameter2, D.max_nbr);
+                           D.cell_spacing2, D.diameter2, D.max_nbr, (uint32_t)(D.p_begin + D.p_count), status);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -512,14 +519,14 @@ __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors_arena(const int32_t* __restrict__ pdom, const DomainParams* __restrict__ doms,
                         const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
                         const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
-                        int32_t n_active)
+                        int32_t n_active, int32_t* __restrict__ status)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
     if (t >= n_active) return;
     const DomainParams& D = doms[pdom[__float_as_uint(ps[t].w)]];
     cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + D.nbr_base, (uint32_t)D.p_begin, D.p_count,
                            D.table_base, D.table_size, ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing,
-                           D.cell_spacing2, D.diameter2, D.max_nbr);
+                           D.cell_spacing2, D.diameter2, D.max_nbr, (uint32_t)n_active, status);
 }
 
 cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pin, int32_t hw,
@@ -531,13 +538,13 @@ cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pi
     if (e != cudaSuccess) return e;
     const int blocks = (hw + kBlock - 1) / kBlock;
     k_hash_keys_arena<<<blocks, kBlock, 0, st>>>(pdom, d.dom, d.p[pin], d.keys, d.vals, hw, sentinel);
-    e = radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot, hw, bits, st);
+    e = radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot, hw, bits, st, d.status);
     if (e != cudaSuccess) return e;
     k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, d.vals, d.p[pin], d.x0, hw, sentinel, d.cell_start,
                                                    d.cell_end, d.ps, d.x0s);
     if (n_active > 0)
         k_cache_neighbors_arena<<<(n_active + kBlock - 1) / kBlock, kBlock, 0, st>>>(
-            pdom, d.dom, d.cell_start, d.cell_end, d.ps, d.x0s, d.nbr, n_active);
+            pdom, d.dom, d.cell_start, d.cell_end, d.ps, d.x0s, d.nbr, n_active, d.status);
     const int passes = (hw > 1 && bits > 0) ? (bits + 7) / 8 : 0;
     if (launches) *launches += 3 + 3 * (uint64_t)passes;
     return cudaGetLastError();
@@ -557,7 +564,7 @@ cudaError_t launch_cache_neighbors(const Launch& L, int pin)
     const DeviceArrays& d = *L.d;
     (void)pin;  // positions come sorted from launch_cell_ranges_gather
     k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.cell_start, d.cell_end, d.ps,
-                                                       d.x0s, d.nbr);
+                                                       d.x0s, d.nbr, d.status);
     return cudaGetLastError();
 }
 

@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kBlock)
 k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
           const ColliderDev* __restrict__ cols, const float4* __restrict__ x,
           const float4* __restrict__ pin, float4* __restrict__ pout,
-          const uint32_t* __restrict__ nbr)
+          const uint32_t* __restrict__ nbr, int32_t* __restrict__ status)
 {
     const Tile tl = tiles[blockIdx.x];
     const int i = tl.begin + (int)threadIdx.x;
@@ -194,6 +194,7 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
         for (int k = 0; k < D.max_nbr; ++k) {
             const uint32_t j = jn;
             if (j == 0xffffffffu) break;
+            if (!VT_IN_RANGE(j, D.p_begin, D.p_begin + D.p_count, status)) break;
             if (k + 1 < D.max_nbr) jn = __ldg(nb + (size_t)(k + 1) * stride);
             const float4 pj4 = pin[j];
             const float denom = wi + pj4.w;
@@ -380,6 +381,7 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
     // constraint as its first endpoint and takes -w_i * common
     for (int e = st_off[i], e1 = st_off[i + 1]; e < e1; ++e) {
         const int2 en = st_ent[e];
+        if (!VT_IN_RANGE(en.x, D.p_begin, D.p_begin + D.p_count, status)) continue;
         vec3 common;
         if (stretch_common(pi4, pin[en.x], __int_as_float(en.y), common)) {
             acc3(acc, common * (-wi));
@@ -523,6 +525,7 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
 
     // 3. particles of the tile
     if (!owns) return;
+    if (!VT_IN_RANGE(i, D.p_begin, D.p_begin + D.p_count, status)) return;
     const int hx = ta + 1, hy = tb + 1;  // this particle's generator (a, b) and halo slot
     const float4 pi4 = sp[hx][hy];
     const vec3 pi = xyz(pi4);
@@ -747,7 +750,7 @@ cudaError_t launch_collide(const Launch& L, int pin, int pout)
 {
     if (!L.n_ptiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
-    k_collide<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.col, d.x, d.p[pin], d.p[pout], d.nbr);
+    k_collide<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.col, d.x, d.p[pin], d.p[pout], d.nbr, d.status);
     return cudaGetLastError();
 }
 

@@ -705,6 +705,10 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
         float ms = 0;
         VT_TRY_CUDA(cudaEventElapsedTime(&ms, s->ev0[prev], s->ev1[prev]), "elapsed");
         ti.frame_ms = ms;
+        if (s->status_pin[prev][0] & vt::VT_STATUS_BOUNDS) {
+            vt::set_error("a device-side bounds check failed (bounds-checked build)");
+            return VT_ERR_STATE;
+        }
         for (const auto& m : s->members[prev]) {
             m.first->done += 1;
             if (s->status_pin[prev][1 + m.second] != 0) m.first->failed = true;  // evicted next tick

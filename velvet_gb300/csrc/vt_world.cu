@@ -832,7 +832,7 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
             VT_STAGE(ST_HASH_KEYS, launch_hash_keys(L, pc), "hash_keys", pk);
             VT_STAGE(ST_RADIX_SORT,
                      radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot,
-                                      n_particles, bits, st),
+                                      n_particles, bits, st, d.status),
                      "radix_sort", 3 * (uint64_t)sort_passes);
             VT_STAGE(ST_CELL_RANGES, launch_cell_ranges_gather(d, pc, n_particles, st), "cell_ranges", 1);
             VT_STAGE(ST_CACHE_NEIGHBORS, launch_cache_neighbors(L, pc), "cache_neighbors", pk);

@@ -32,6 +32,28 @@
 
 namespace vt {
 
+// Bounds-checked builds (-DVT_CHECKED=1: libvelvet_gb300_checked.so, made by build()
+// beside the production library): data-dependent indices — neighbour and constraint
+// entries, sorted-slot ranges, scatter positions — are range-checked before use; a
+// failure sets VT_STATUS_BOUNDS in the status word (vt_solver_sync, vt_batch_sync and
+// vt_server_tick then return VT_ERR_STATE) and the access is skipped.  The production
+// build compiles the checks away.  (Stands in for a sanitizer, which is not available.)
+#ifndef VT_CHECKED
+#define VT_CHECKED 0
+#endif
+constexpr int32_t VT_STATUS_NONFINITE = 1, VT_STATUS_BOUNDS = 2;
+#if VT_CHECKED
+__device__ __forceinline__ bool vt_in_range(long long v, long long lo, long long hi, int32_t* status)
+{
+    if (v >= lo && v < hi) return true;
+    if (status) atomicOr(status, VT_STATUS_BOUNDS);
+    return false;
+}
+#define VT_IN_RANGE(v, lo, hi, status) vt_in_range((long long)(v), (long long)(lo), (long long)(hi), (status))
+#else
+#define VT_IN_RANGE(v, lo, hi, status) true
+#endif
+
 // Per-domain parameters, rewritten on the device before every frame.
 struct DomainParams {
     int32_t p_begin, p_count;      // particle range
@@ -205,7 +227,7 @@ cudaError_t launch_hash_keys(const Launch& L, int pin);
 // result lands in keys / vals.  Scratch: keys_tmp, vals_tmp, hist, digit_tot.
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
                              uint32_t* vals_tmp, uint32_t* hist, uint32_t* digit_tot,
-                             int32_t n, int32_t bits, cudaStream_t st);
+                             int32_t n, int32_t bits, cudaStream_t st, int32_t* status = nullptr);
 size_t radix_hist_words(int32_t n);  // size of `hist` for n items
 cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_start,
                                uint32_t* cell_end, cudaStream_t st);
