@@ -255,6 +255,12 @@ vt_status vt_solver_launch_count(const vt_solver* s, uint64_t* out);
  * directly, as the reference does. */
 vt_status vt_solver_use_graphs(vt_solver* s, int32_t on);
 
+/* 1 (default): a cloth built by vt_cloth_build_grid_constraints is solved by the
+ * implicit-topology tile kernel; 0: by the general CSR kernels, from the constraint lists
+ * the builder generated.  Results are identical either way (a cross-check of the two
+ * kernels); the next simulate rebuilds the device state. */
+vt_status vt_solver_use_grid_kernel(vt_solver* s, int32_t on);
+
 /* ------------------------------------------------------------------ checkpoint / resume
  * The simulation state of a solver as one flat binary (no reference counterpart; a reset
  * there re-runs the scene): a 16-byte header (magic "VTCK", version 1, particle count,

@@ -189,6 +189,7 @@ SIGNATURES: dict[str, tuple] = {
     "vt_solver_state_save": (I32, [P, P, U64]),
     "vt_solver_state_load": (I32, [P, P, U64]),
     "vt_solver_use_graphs": (I32, [P, I32]),
+    "vt_solver_use_grid_kernel": (I32, [P, I32]),
     "vt_batch_create": (I32, [C.POINTER(P)]),
     "vt_batch_destroy": (I32, [P]),
     "vt_batch_add": (I32, [P, P, PI32]),

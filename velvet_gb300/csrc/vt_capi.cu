@@ -808,6 +808,18 @@ vt_status vt_solver_use_graphs(vt_solver* s, int32_t on)
     return VT_OK;
 }
 
+vt_status vt_solver_use_grid_kernel(vt_solver* s, int32_t on)
+{
+    VT_CHECK(s, VT_ERR_INVALID_ARGUMENT, "NULL solver");
+    VT_GUARD_BEGIN
+    if (s->h.use_grid_kernel == (on != 0)) return VT_OK;
+    vt_status st = make_topology_change(s);  // the device world is rebuilt at the next simulate
+    if (st != VT_OK) return st;
+    s->h.use_grid_kernel = on != 0;
+    return VT_OK;
+    VT_GUARD_END
+}
+
 vt_status vt_tuning_set_grid_tile(int32_t variant) { return vt::tuning_force(variant); }
 
 vt_status vt_solver_grid_tile(const vt_solver* s, int32_t* variant)
