@@ -769,8 +769,7 @@ def main() -> None:
     ncol = sum(len(c.colliders(0)) for c in wl.cloths)
     h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
     d2h = n_tot * 24
-    grid_tile = (["7x31", "15x15", "3x63"][batch.grid_tile() % 3] + (" x5/SM" if batch.grid_tile() >= 3 else " x4/SM")
-                 if batch.grid_tile() >= 0 else None)
+    grid_tile = vg.grid_variant_name(batch.grid_tile())
     batch.close()
 
     # ---- the plain drop-in solver on the same workload, one cloth at a time

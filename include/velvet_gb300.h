@@ -456,10 +456,10 @@ vt_status vt_batch_render(vt_batch* b, const vt_render_params* rp, uint32_t* rgb
                           void* stream);
 
 /* ------------------------------------------------------------------ tuning
- * The grid-cloth kernel has several tile shapes; on its first frame a solver, batch or
+ * The grid-cloth kernel has several variants; on its first frame a solver, batch or
  * server times them on its own cloths and keeps the fastest (decisions are cached per
- * size signature for the process).  The shape never changes a result.  This forces one
- * shape for all handles created or tuned afterwards: 0 = 7x31, 1 = 15x15, 2 = 3x63 at
+ * size signature for the process).  The variant never changes a result.  This forces one
+ * for all handles created or tuned afterwards: 0 = 7x31, 1 = 15x15, 2 = 3x63 tiles at
  * four resident blocks per SM, 3-5 the same shapes at five; -1 returns to autotuning. */
 vt_status vt_tuning_set_grid_tile(int32_t variant);
 /* The shape in use by a solver / batch (after its first frame). */

@@ -92,38 +92,48 @@ def test_grid_tiles_at_every_edge_case(tile_edge):
     same(g.velocities(), o.velocities(), f"side {tile_edge} velocities")
 
 
-@pytest.mark.parametrize("variant", range(6))
-def test_every_grid_tile_shape_gives_the_same_bits(variant):
+@pytest.mark.parametrize("side", [37, 64])
+@pytest.mark.parametrize("variant", range(len(vg.GRID_VARIANTS)))
+def test_every_grid_tile_shape_gives_the_same_bits(variant, side):
     """The autotuner chooses among tile shapes and occupancies; each must reproduce the
-    oracle exactly."""
+    oracle exactly.  Sides of 37 and 64 vertices leave partial tiles for every shape (64:
+    a last row of tiles one particle high for 7x31 and 3x63, a last column one wide for
+    3x63)."""
     import ctypes as C
 
     assert vg.lib().vt_tuning_set_grid_tile(variant) == 0
     try:
-        spec = spec_of(37, 0.4)  # 37 leaves partial tiles for every shape
+        spec = spec_of(side, 0.4)
         o, g = Oracle(), vg.ClothSolver()
         for s in (o, g):
             W.build_plain(spec, s)
         run_frames([o, g], spec, 4)
-        same(g.positions(), o.positions(), f"tile shape {variant}")
+        same(g.positions(), o.positions(), f"tile shape {variant}, side {side}")
+        same(g.velocities(), o.velocities(), f"tile shape {variant}, side {side} velocities")
         used = C.c_int32()
         assert vg.lib().vt_solver_grid_tile(g.handle, C.byref(used)) == 0 and used.value == variant
     finally:
         vg.lib().vt_tuning_set_grid_tile(-1)
 
 
+@pytest.mark.parametrize("variant", [-1, 1, 5])
 @pytest.mark.parametrize("n_slots", [5, 24])
-def test_many_lra_slots_recompute_their_rests(n_slots):
+def test_many_lra_slots_recompute_their_rests(n_slots, variant):
     """More attach slots than the per-particle cache holds (the stress configuration
-    attaches a whole row): the tile kernel recomputes |slot0 - x0| for each slot."""
-    side = 24
-    spec = spec_of(side, 0.4, attached=list(range(0, side, side // n_slots))[:n_slots])
-    o, g = Oracle(), vg.ClothSolver()
-    for s in (o, g):
-        W.build_plain(spec, s)
-    run_frames([o, g], spec, 5)
-    same(g.positions(), o.positions(), f"{n_slots} LRA slots")
-    same(g.velocities(), o.velocities(), f"{n_slots} LRA slots velocities")
+    attaches a whole row): the tile kernel recomputes |slot0 - x0| for each slot, at four
+    and at five resident blocks per SM."""
+    assert vg.lib().vt_tuning_set_grid_tile(variant) == 0
+    try:
+        side = 24
+        spec = spec_of(side, 0.4, attached=list(range(0, side, side // n_slots))[:n_slots])
+        o, g = Oracle(), vg.ClothSolver()
+        for s in (o, g):
+            W.build_plain(spec, s)
+        run_frames([o, g], spec, 5)
+        same(g.positions(), o.positions(), f"{n_slots} LRA slots")
+        same(g.velocities(), o.velocities(), f"{n_slots} LRA slots velocities")
+    finally:
+        vg.lib().vt_tuning_set_grid_tile(-1)
 
 
 def checkerboard_mesh(res, size):

@@ -7,10 +7,10 @@ the benchmark use.  Nothing here computes physics on the CPU: if the library is 
 every call raises.
 """
 from ._abi import VtError, VtParams, VtSdfCollider, default_params, lib  # noqa: F401
-from .solver import (BatchSolver, ClothServer, ClothSolver, colmajor, hash_objects, render_params,  # noqa: F401
-                     rgba_to_rgb, stream_handle, write_ppm)
+from .solver import (GRID_VARIANTS, BatchSolver, ClothServer, ClothSolver, colmajor,  # noqa: F401
+                     grid_variant_name, hash_objects, render_params, rgba_to_rgb, stream_handle, write_ppm)
 
 __all__ = [
     "BatchSolver", "ClothServer", "ClothSolver", "VtError", "VtParams", "VtSdfCollider", "default_params", "lib",
-    "colmajor", "hash_objects", "stream_handle",
+    "colmajor", "hash_objects", "stream_handle", "GRID_VARIANTS", "grid_variant_name",
 ]

@@ -137,7 +137,7 @@ public:
     int32_t n_domains = 0, n_particles = 0, n_bends = 0, n_slots = 0, n_cols = 0;
     int32_t total_keys = 0, n_ptiles = 0, n_btiles = 0, nbr_words = 0;
     int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
-    int32_t grid_variant = 0;  // tile shape of the grid kernel (kGridShape index)
+    int32_t grid_variant = 0;  // tile shape of the grid kernel (kGridVariant index)
     // Times every grid tile shape on this world's cloths (one Jacobi iteration each, from
     // the current positions, into scratch buffers) and keeps the fastest; decisions are
     // cached per size signature for the process.  Never changes a result.

@@ -20,6 +20,8 @@
 //     pre-stabilisation CollideSDF is fused with the first PredictPositions.
 //   * float4 particles (w = inverse mass) so each particle is one 16-byte load.
 // Also here: the device grid builder (k_grid_build) and read-back packing (k_pack_xyz).
+#include <utility>
+
 #include "vt_math.cuh"
 #include "vt_world.h"
 
@@ -421,15 +423,120 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
 // constraint order x-major / y / type (VtClothObjectGPU.hpp:75-116), bending of quad
 // (x, y) over ((x,y), (x+1,y+1), (x,y+1), (x+1,y)) (:118-132), rest lengths
 // |x0_i - x0_j| (the builder's values: registration verifies x == x0 at build time)
-// and rest angles 0.  A block owns a 7 x 31 tile; it stages the tile and a one-particle
-// halo of predicted positions in shared memory, evaluates each of the 8 x 32
+// and rest angles 0.  The rest lengths |x0_i - x0_j| of a generator's four constraints
+// (grest) and a particle's LRA rest distances (glra, up to kGridLraCached slots) are
+// evaluated once at registration with the same FP32 operations instead of every
+// iteration: the kernels are bound by instruction issue, HBM is mostly idle.
+
+// Generator (X, Y) of a grid cloth of R x R quads: its stretch constraints t0..t3 (rests
+// rest.x .. rest.w) and the bend of quad (X, Y), from the predicted position of (X, Y) at
+// sp[hx][hy] and of (X,Y+1), (X+1,Y), (X+1,Y+1) beside it.  Each stretch result goes to
+// sst[t][gx][gy] (lambda * gradient, w = 1 when it fired) and each bending corner to
+// sbd[c][gx][gy] as soon as it is known; a generator outside the cloth writes zeros.
+template <int kHB, int kGA, int kGB>
+__device__ __forceinline__ void grid_generator(int X, int Y, int R, const float4 (*sp)[kHB], int hx, int hy,
+                                               float4 (*sst)[kGA][kGB], float4 (*sbd)[kGA][kGB], int gx,
+                                               int gy, float4 rest, float xpbd)
+{
+    const float4 zero = make_float4(0, 0, 0, 0);
+    const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
+    const bool full = gen && X < R && Y < R;
+    const float4 pxy = sp[hx][hy];
+    vec3 cm;
+    float4 r = zero;
+    if (gen && Y < R && stretch_common(pxy, sp[hx][hy + 1], rest.x, cm))  // t0: (x,y)-(x,y+1)
+        r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+    sst[0][gx][gy] = r;
+    r = zero;
+    if (gen && X < R && stretch_common(pxy, sp[hx + 1][hy], rest.y, cm))  // t1: (x,y)-(x+1,y)
+        r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+    sst[1][gx][gy] = r;
+    r = zero;
+    if (full && stretch_common(pxy, sp[hx + 1][hy + 1], rest.z, cm))  // t2: (x,y)-(x+1,y+1)
+        r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+    sst[2][gx][gy] = r;
+    r = zero;
+    if (full && stretch_common(sp[hx][hy + 1], sp[hx + 1][hy], rest.w, cm))  // t3: (x,y+1)-(x+1,y)
+        r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+    sst[3][gx][gy] = r;
+    float4 c0 = zero, c1 = zero, c2 = zero, c3 = zero;
+    if (full)  // bend of quad (x, y): corners (x,y), (x+1,y+1), (x,y+1), (x+1,y)
+        bend_eval(pxy, sp[hx + 1][hy + 1], sp[hx][hy + 1], sp[hx + 1][hy], 0.0f, xpbd, c0, c1, c2, c3);
+    sbd[0][gx][gy] = c0;
+    sbd[1][gx][gy] = c1;
+    sbd[2][gx][gy] = c2;
+    sbd[3][gx][gy] = c3;
+}
+
+// The Jacobi sum of grid particle (a, b), i = its index: its eight stretch constraints,
+// its LRA attachments in slot order, its four bending corners, all in constraint order.
+// Generator (a, b)'s results sit at [gx][gy] of sst / sbd, generator (a-1, b-1)'s at
+// [gx-1][gy-1].  gl: the particle's cached LRA rest distances, sslot: the cached slots.
+template <int kGA, int kGB>
+__device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, int gx, int gy,
+                                                  const float4 (*sst)[kGA][kGB], const float4 (*sbd)[kGA][kGB],
+                                                  vec3 pi, float wi, int ns, int s0, const float4* gl,
+                                                  const float4* sslot, const float4* __restrict__ x0,
+                                                  const float4* __restrict__ slots,
+                                                  const float4* __restrict__ slots0, float lrs, vec3& acc,
+                                                  int& cnt)
+{
+    const float nw = -wi;
+#define VT_TAKE(s4, scale)                          \
+    do {                                            \
+        const float4 s_ = (s4);                     \
+        if (s_.w != 0.0f) {                         \
+            acc3(acc, mk3(s_.x, s_.y, s_.z) * (scale)); \
+            cnt++;                                  \
+        }                                           \
+    } while (0)
+    // stretch, constraint order: generators (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
+    if (a >= 1 && b >= 1) VT_TAKE(sst[2][gx - 1][gy - 1], wi);  // t2, second endpoint
+    if (a >= 1) VT_TAKE(sst[1][gx - 1][gy], wi);                // t1, second endpoint
+    if (a >= 1 && b < R) VT_TAKE(sst[3][gx - 1][gy], wi);       // t3, second endpoint
+    if (b >= 1) VT_TAKE(sst[0][gx][gy - 1], wi);                // t0, second endpoint
+    if (b >= 1 && a < R) VT_TAKE(sst[3][gx][gy - 1], nw);       // t3, first endpoint
+    if (b < R) VT_TAKE(sst[0][gx][gy], nw);                     // t0, first endpoint
+    if (a < R) VT_TAKE(sst[1][gx][gy], nw);                     // t1, first endpoint
+    if (a < R && b < R) VT_TAKE(sst[2][gx][gy], nw);            // t2, first endpoint
+#undef VT_TAKE
+    // long-range attachments, slot order
+    if (ns) {
+        if (ns <= kGridLraCached) {
+            const float4 r4 = *gl;
+            const float rs[4] = {r4.x, r4.y, r4.z, r4.w};
+#pragma unroll
+            for (int k = 0; k < kGridLraCached; ++k)
+                if (k < ns) attach_one(pi, wi, xyz(sslot[k]), rs[k] * lrs, acc, cnt);
+        } else {
+            const vec3 x0i = xyz(x0[i]);
+            for (int s = s0; s < s0 + ns; ++s) {
+                const float rest = length(xyz(slots0[s]) - x0i);
+                attach_one(pi, wi, xyz(slots[s]), rest * lrs, acc, cnt);
+            }
+        }
+    }
+    // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
+#define VT_CORNER(c4)                     \
+    do {                                  \
+        const float4 c_ = (c4);           \
+        if (c_.w != 0.0f) {               \
+            acc3(acc, xyz(c_));           \
+            cnt++;                        \
+        }                                 \
+    } while (0)
+    if (a >= 1 && b >= 1) VT_CORNER(sbd[1][gx - 1][gy - 1]);
+    if (a >= 1 && b < R) VT_CORNER(sbd[3][gx - 1][gy]);
+    if (a < R && b >= 1) VT_CORNER(sbd[2][gx][gy - 1]);
+    if (a < R && b < R) VT_CORNER(sbd[0][gx][gy]);
+#undef VT_CORNER
+}
+
+// The tile kernel: a block owns a TA x TB tile; it stages the tile and a one-particle
+// halo of predicted positions in shared memory, evaluates each of the (TA+1) x (TB+1)
 // generators touching the tile once (one per thread: one bend + four stretch
-// constraints), then each particle sums its eight stretch, the LRA and its four bending
-// corrections in constraint order — the order of the CSR kernel and of the oracle.
-// The rest lengths |x0_i - x0_j| of a generator's four constraints (grest) and a
-// particle's LRA rest distances (glra, up to kGridLraCached slots) are evaluated once
-// at registration with the same FP32 operations instead of every iteration: the kernel
-// is bound by instruction issue, HBM is mostly idle.
+// constraints), then each particle sums its results in constraint order — the order of
+// the CSR kernel and of the oracle.
 template <int kMode, int kTA, int kTB, int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks)
 k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__ doms,
@@ -438,7 +545,6 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
             const float4* __restrict__ glra, const float4* __restrict__ slots,
             const float4* __restrict__ slots0, int32_t* __restrict__ status)
 {
-    constexpr int kGridTA = kTA, kGridTB = kTB;
     constexpr int kGHA = kTA + 2, kGHB = kTB + 2;  // halo tile
     constexpr int kGGA = kTA + 1, kGGB = kTB + 1;  // generators, kGGA * kGGB == kBlock
     static_assert(kGGA * kGGB == kBlock, "one generator per thread");
@@ -459,9 +565,9 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     const int ns = tl.slot_count, s0 = tl.slot_begin;
     const int a0 = tl.a0, b0 = tl.b0;
     const int gx = tid / kGGB, gy = tid - gx * kGGB;  // this thread's generator
-    const int ta = tid / kGridTB, tb = tid - ta * kGridTB;  // this thread's particle
+    const int ta = tid / kTB, tb = tid - ta * kTB;    // this thread's particle
     const int a = a0 + ta, b = b0 + tb;
-    const bool owns = tid < kGridTA * kGridTB && a < V && b < V;
+    const bool owns = tid < kTA * kTB && a < V && b < V;
     const int i = base + a * V + b;
 
     // 1. stage with asynchronous copies (no registers held across the wait): the halo
@@ -487,40 +593,10 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     __syncthreads();
     const DomainParams& D = sdom;
 
-    // 2. generators (x, y) = (a0 - 1 + gx, b0 - 1 + gy): one per thread; each result goes
-    // to shared memory as soon as it is known
-    {
-        const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
-        const float4 zero = make_float4(0, 0, 0, 0);
-        const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
-        const bool full = gen && X < R && Y < R;
-        const float4 pxy = sp[gx][gy];
-        const float4 rest = sgr[tid];  // read before sst[0][gx][gy] (the same slot) is written
-        vec3 cm;
-        float4 r = zero;
-        if (gen && Y < R && stretch_common(pxy, sp[gx][gy + 1], rest.x, cm))  // t0: (x,y)-(x,y+1)
-            r = make_float4(cm.x, cm.y, cm.z, 1.0f);
-        sst[0][gx][gy] = r;
-        r = zero;
-        if (gen && X < R && stretch_common(pxy, sp[gx + 1][gy], rest.y, cm))  // t1: (x,y)-(x+1,y)
-            r = make_float4(cm.x, cm.y, cm.z, 1.0f);
-        sst[1][gx][gy] = r;
-        r = zero;
-        if (full && stretch_common(pxy, sp[gx + 1][gy + 1], rest.z, cm))  // t2: (x,y)-(x+1,y+1)
-            r = make_float4(cm.x, cm.y, cm.z, 1.0f);
-        sst[2][gx][gy] = r;
-        r = zero;
-        if (full && stretch_common(sp[gx][gy + 1], sp[gx + 1][gy], rest.w, cm))  // t3: (x,y+1)-(x+1,y)
-            r = make_float4(cm.x, cm.y, cm.z, 1.0f);
-        sst[3][gx][gy] = r;
-        float4 c0 = zero, c1 = zero, c2 = zero, c3 = zero;
-        if (full)  // bend of quad (x, y): corners (x,y), (x+1,y+1), (x,y+1), (x+1,y)
-            bend_eval(pxy, sp[gx + 1][gy + 1], sp[gx][gy + 1], sp[gx + 1][gy], 0.0f, D.xpbd_bend, c0, c1, c2, c3);
-        sbd[0][gx][gy] = c0;
-        sbd[1][gx][gy] = c1;
-        sbd[2][gx][gy] = c2;
-        sbd[3][gx][gy] = c3;
-    }
+    // 2. generators (x, y) = (a0 - 1 + gx, b0 - 1 + gy): one per thread (the rests are
+    // read before sst[0][gx][gy], the same slot, is written)
+    grid_generator<kGHB, kGGA, kGGB>(a0 - 1 + gx, b0 - 1 + gy, R, sp, gx, gy, sst, sbd, gx, gy, sgr[tid],
+                                     D.xpbd_bend);
     __syncthreads();
 
     // 3. particles of the tile
@@ -529,57 +605,11 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     const int hx = ta + 1, hy = tb + 1;  // this particle's generator (a, b) and halo slot
     const float4 pi4 = sp[hx][hy];
     const vec3 pi = xyz(pi4);
-    const float wi = pi4.w, nw = -wi;
+    const float wi = pi4.w;
     vec3 acc = mk3(0, 0, 0);
     int cnt = 0;
-#define VT_TAKE(s4, scale)                          \
-    do {                                            \
-        const float4 s_ = (s4);                     \
-        if (s_.w != 0.0f) {                         \
-            acc3(acc, mk3(s_.x, s_.y, s_.z) * (scale)); \
-            cnt++;                                  \
-        }                                           \
-    } while (0)
-    // stretch, constraint order: generators (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
-    if (a >= 1 && b >= 1) VT_TAKE(sst[2][hx - 1][hy - 1], wi);  // t2, second endpoint
-    if (a >= 1) VT_TAKE(sst[1][hx - 1][hy], wi);                // t1, second endpoint
-    if (a >= 1 && b < R) VT_TAKE(sst[3][hx - 1][hy], wi);       // t3, second endpoint
-    if (b >= 1) VT_TAKE(sst[0][hx][hy - 1], wi);                // t0, second endpoint
-    if (b >= 1 && a < R) VT_TAKE(sst[3][hx][hy - 1], nw);       // t3, first endpoint
-    if (b < R) VT_TAKE(sst[0][hx][hy], nw);                     // t0, first endpoint
-    if (a < R) VT_TAKE(sst[1][hx][hy], nw);                     // t1, first endpoint
-    if (a < R && b < R) VT_TAKE(sst[2][hx][hy], nw);            // t2, first endpoint
-#undef VT_TAKE
-    // long-range attachments, slot order
-    if (ns) {
-        if (ns <= kGridLraCached) {
-            const float4 r4 = sgl[tid];
-            const float rs[4] = {r4.x, r4.y, r4.z, r4.w};
-#pragma unroll
-            for (int k = 0; k < kGridLraCached; ++k)
-                if (k < ns) attach_one(pi, wi, xyz(sslot[k]), rs[k] * D.lrs, acc, cnt);
-        } else {
-            const vec3 x0i = xyz(x0[i]);
-            for (int s = s0; s < s0 + ns; ++s) {
-                const float rest = length(xyz(slots0[s]) - x0i);
-                attach_one(pi, wi, xyz(slots[s]), rest * D.lrs, acc, cnt);
-            }
-        }
-    }
-    // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
-#define VT_CORNER(c4)                     \
-    do {                                  \
-        const float4 c_ = (c4);           \
-        if (c_.w != 0.0f) {               \
-            acc3(acc, xyz(c_));           \
-            cnt++;                        \
-        }                                 \
-    } while (0)
-    if (a >= 1 && b >= 1) VT_CORNER(sbd[1][hx - 1][hy - 1]);
-    if (a >= 1 && b < R) VT_CORNER(sbd[3][hx - 1][hy]);
-    if (a < R && b >= 1) VT_CORNER(sbd[2][hx][hy - 1]);
-    if (a < R && b < R) VT_CORNER(sbd[0][hx][hy]);
-#undef VT_CORNER
+    grid_particle_sum<kGGA, kGGB>(a, b, R, i, hx, hy, sst, sbd, pi, wi, ns, s0, &sgl[tid], sslot, x0, slots,
+                                  slots0, D.lrs, acc, cnt);
     apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, &sx[tid], pout, x, v, status);
 }
 
@@ -779,60 +809,66 @@ cudaError_t launch_solve(const Launch& L, int pin, int pout, int mode)
     return cudaGetLastError();
 }
 
-template <int kMode, int kTA, int kTB, int kMinBlocks>
-static cudaError_t carveout()
+template <typename K>
+static cudaError_t carveout(K kernel)
 {
-    return cudaFuncSetAttribute(k_grid_iter<kMode, kTA, kTB, kMinBlocks>,
-                                cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
 }
 
-template <int kTA, int kTB>
-static cudaError_t carveout_modes()
+// every (mode, occupancy) instance variant v launches
+template <int v>
+static cudaError_t carveout_variant()
 {
-    cudaError_t e = carveout<SOLVE_PLAIN, kTA, kTB, 4>();
-    if (e == cudaSuccess) e = carveout<SOLVE_PLAIN, kTA, kTB, 5>();
-    if (e == cudaSuccess) e = carveout<SOLVE_FINALIZE, kTA, kTB, 4>();
-    if (e == cudaSuccess) e = carveout<SOLVE_FINALIZE_PREDICT, kTA, kTB, 4>();
+    constexpr GridVariant g = kGridVariant[v];
+    cudaError_t e = carveout(k_grid_iter<SOLVE_PLAIN, g.ta, g.tb, g.blocks>);
+    if (e == cudaSuccess) e = carveout(k_grid_iter<SOLVE_FINALIZE, g.ta, g.tb, 4>);
+    if (e == cudaSuccess) e = carveout(k_grid_iter<SOLVE_FINALIZE_PREDICT, g.ta, g.tb, 4>);
+    return e;
+}
+
+template <int... V>
+static cudaError_t carveout_all(std::integer_sequence<int, V...>)
+{
+    cudaError_t e = cudaSuccess;
+    ((e = e == cudaSuccess ? carveout_variant<V>() : e), ...);
     return e;
 }
 
 cudaError_t prepare_kernels()
 {
     // most shared memory per SM for the tile kernel: more resident tiles per SM
-    cudaError_t e = carveout_modes<kGridShape[0].ta, kGridShape[0].tb>();
-    if (e == cudaSuccess) e = carveout_modes<kGridShape[1].ta, kGridShape[1].tb>();
-    if (e == cudaSuccess) e = carveout_modes<kGridShape[2].ta, kGridShape[2].tb>();
-    return e;
+    return carveout_all(std::make_integer_sequence<int, kGridVariants>{});
 }
 
 // The plain iterations (nine in ten launches) use the variant's occupancy; the finalizing
 // ones always the four-block build.
-template <int kTA, int kTB, int kMinBlocks>
-static void grid_iter_shape(const Launch& L, int pin, int pout, int mode)
+template <int v>
+static void grid_iter_variant(const Launch& L, int pin, int pout, int mode)
 {
+    constexpr GridVariant g = kGridVariant[v];
     const DeviceArrays& d = *L.d;
 #define VT_GRID_ARGS \
     d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.grest, d.glra, d.slots, d.slots0, d.status
     if (mode == SOLVE_PLAIN)
-        k_grid_iter<SOLVE_PLAIN, kTA, kTB, kMinBlocks><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+        k_grid_iter<SOLVE_PLAIN, g.ta, g.tb, g.blocks><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
     else if (mode == SOLVE_FINALIZE)
-        k_grid_iter<SOLVE_FINALIZE, kTA, kTB, 4><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+        k_grid_iter<SOLVE_FINALIZE, g.ta, g.tb, 4><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
     else
-        k_grid_iter<SOLVE_FINALIZE_PREDICT, kTA, kTB, 4><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
+        k_grid_iter<SOLVE_FINALIZE_PREDICT, g.ta, g.tb, 4><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
 #undef VT_GRID_ARGS
+}
+
+template <int... V>
+static void grid_iter_dispatch(const Launch& L, int pin, int pout, int mode, std::integer_sequence<int, V...>)
+{
+    ((L.grid_variant == V ? grid_iter_variant<V>(L, pin, pout, mode) : void()), ...);
 }
 
 cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int mode)
 {
     if (!L.n_gtiles) return cudaSuccess;
-    switch (L.grid_variant) {
-    case 1: grid_iter_shape<kGridShape[1].ta, kGridShape[1].tb, 4>(L, pin, pout, mode); break;
-    case 2: grid_iter_shape<kGridShape[2].ta, kGridShape[2].tb, 4>(L, pin, pout, mode); break;
-    case 3: grid_iter_shape<kGridShape[0].ta, kGridShape[0].tb, 5>(L, pin, pout, mode); break;
-    case 4: grid_iter_shape<kGridShape[1].ta, kGridShape[1].tb, 5>(L, pin, pout, mode); break;
-    case 5: grid_iter_shape<kGridShape[2].ta, kGridShape[2].tb, 5>(L, pin, pout, mode); break;
-    default: grid_iter_shape<kGridShape[0].ta, kGridShape[0].tb, 4>(L, pin, pout, mode); break;
-    }
+    if (L.grid_variant < 0 || L.grid_variant >= kGridVariants) return cudaErrorInvalidValue;
+    grid_iter_dispatch(L, pin, pout, mode, std::make_integer_sequence<int, kGridVariants>{});
     return cudaGetLastError();
 }
 

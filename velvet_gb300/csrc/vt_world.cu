@@ -542,9 +542,9 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         nwb += h.P.max_num_neighbors * n;
         cb += (int32_t)h.colliders.size();
     }
-    // grid tiles of the shape to start with; capacity for the largest shape
+    // grid tiles of the variant to start with; capacity for the variant with the most
     gtiles_cap_ = 0;
-    for (int v = 0; v < kGridShapes; ++v) {
+    for (int v = 0; v < kGridVariants; ++v) {
         std::vector<GridTile> tmp;
         for (auto& gd : grid_doms_) grid_tiles_for(tmp, gd.first, hdom[gd.first], v);
         gtiles_cap_ = std::max(gtiles_cap_, (int32_t)tmp.size());

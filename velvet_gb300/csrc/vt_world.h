@@ -92,26 +92,23 @@ struct GridTile {
     int32_t dom, a0, b0, res;
     int32_t p_begin, slot_begin, slot_count, pad_;
 };
-// Tile shapes of the grid kernel; every shape has (TA+1) x (TB+1) = 256 generators, one
-// per thread.  The shape changes which block computes what, never a result.
-struct GridShape {
-    int ta, tb;
+// Variants of the tile kernel: a tile shape, every one with (TA+1) x (TB+1) = 256
+// generators (one per thread), and the resident blocks per SM its plain Jacobi
+// iterations are compiled for (four: 64 registers; five: 48, the shared-memory
+// footprint allows five).  The variant changes which block computes what, never a result.
+struct GridVariant {
+    int ta, tb, blocks;
 };
-constexpr int kGridShapes = 3;
-constexpr GridShape kGridShape[kGridShapes] = {{7, 31}, {15, 15}, {3, 63}};
-// A tile-kernel variant is a shape and the resident blocks per SM its plain Jacobi
-// iterations are compiled for: variants 0-2 four blocks (64 registers), 3-5 five blocks
-// (48 registers; the shared-memory footprint allows five).  Results never differ.
-constexpr int kGridVariants = 2 * kGridShapes;
-constexpr int grid_shape_of(int variant) { return variant % kGridShapes; }
-constexpr int kGridTA = 7, kGridTB = 31;  // shape 0
-// Tiles of shape `variant` covering the (grid_res+1)^2 grid cloth of domain `dom`.
+constexpr int kGridVariants = 6;
+constexpr GridVariant kGridVariant[kGridVariants] = {{7, 31, 4}, {15, 15, 4}, {3, 63, 4},
+                                                     {7, 31, 5}, {15, 15, 5}, {3, 63, 5}};
+// Tiles of variant `variant` covering the (grid_res+1)^2 grid cloth of domain `dom`.
 inline void grid_tiles_for(std::vector<GridTile>& out, int dom, const DomainParams& D, int variant)
 {
-    const int sh = grid_shape_of(variant);
-    const int V = D.grid_res + 1, ta = kGridShape[sh].ta, tb = kGridShape[sh].tb;
-    for (int a = 0; a < V; a += ta)
-        for (int b = 0; b < V; b += tb)
+    const GridVariant g = kGridVariant[variant];
+    const int V = D.grid_res + 1;
+    for (int a = 0; a < V; a += g.ta)
+        for (int b = 0; b < V; b += g.tb)
             out.push_back(GridTile{dom, a, b, D.grid_res, D.p_begin, D.grid_slot_begin, D.grid_slot_count, 0});
 }
 
@@ -180,7 +177,7 @@ struct Launch {
     int32_t n_particles;
     cudaStream_t st;
     int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
-    int32_t grid_variant = 0;  // tile shape of the gtiles (kGridShape index)
+    int32_t grid_variant = 0;  // grid kernel variant of the gtiles (kGridVariant index)
 };
 
 // One grid cloth built on the device: GenerateClothMesh + AddCloth (positions, inverse

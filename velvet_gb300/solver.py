@@ -8,7 +8,7 @@ Every call goes through libvelvet_gb300.so; a failing status raises VtError.
 from __future__ import annotations
 
 import ctypes as C
-from typing import Iterable, Sequence
+from typing import Iterable, Optional, Sequence
 
 import numpy as np
 
@@ -67,6 +67,19 @@ def write_ppm(path, img: np.ndarray) -> None:
     with open(path, "wb") as f:
         f.write(b"P6\n%d %d\n255\n" % (rgb.shape[1], rgb.shape[0]))
         f.write(rgb.tobytes())
+
+
+# Variants of the grid tile kernel, by index (vt_tuning_set_grid_tile): (tile rows, tile
+# columns, resident blocks per SM).
+GRID_VARIANTS = ((7, 31, 4), (15, 15, 4), (3, 63, 4), (7, 31, 5), (15, 15, 5), (3, 63, 5))
+
+
+def grid_variant_name(v: int) -> Optional[str]:
+    """'15x15 x4/SM', or None for -1 (not chosen yet)."""
+    if v < 0:
+        return None
+    ta, tb, blocks = GRID_VARIANTS[v]
+    return f"{ta}x{tb} x{blocks}/SM"
 
 
 class ClothSolver:
@@ -223,7 +236,7 @@ class ClothSolver:
         check(lib().vt_attach_slot_set(self._h, slot, _ptr(a)), "vt_attach_slot_set")
 
     def grid_tile(self) -> int:
-        """Tile shape the grid kernel uses (-1 before the first simulate)."""
+        """Grid kernel variant in use (an index of GRID_VARIANTS; -1 before the first simulate)."""
         v = C.c_int32()
         check(lib().vt_solver_grid_tile(self._h, C.byref(v)), "vt_solver_grid_tile")
         return v.value
@@ -362,7 +375,7 @@ class BatchSolver:
         check(lib().vt_batch_use_graphs(self._h, 1 if on else 0), "vt_batch_use_graphs")
 
     def grid_tile(self) -> int:
-        """Tile shape the grid kernel uses (-1 before the first simulate)."""
+        """Grid kernel variant in use (an index of GRID_VARIANTS; -1 before the first simulate)."""
         v = C.c_int32()
         check(lib().vt_batch_grid_tile(self._h, C.byref(v)), "vt_batch_grid_tile")
         return v.value
