@@ -92,6 +92,33 @@ def iteration_bytes(wl) -> float:
     return b
 
 
+# FP32 operations per (particle, LRA slot) pair of an iteration when the rest distance is
+# recomputed: |slot0 - x0| (3 sub, 3 mul, 2 add, sqrt), times the stretchiness, the
+# inverse-mass test, |p - slot| (3 sub, 3 mul, 2 add, sqrt) and the comparison.
+LRA_OPS_PER_PAIR = 21
+GRID_LRA_CACHED = 4  # slots whose rest distances the tile kernel keeps per particle
+
+
+def lra_fp32_roofline(wl, t_iter_ms: float, clock_info) -> dict | None:
+    """Cloths with more LRA slots than the tile kernel caches (the stress configuration's
+    whole attached row) make the iteration a loop of FP32 arithmetic per (particle, slot)
+    pair: reported against the FP32 issue rate of the SMs at the sampled clock (one
+    unfused FP32 operation per lane per cycle, 128 lanes per SM)."""
+    import torch
+
+    pairs = sum(c.side * c.side * len(c.attached) for c in wl.cloths if len(c.attached) > GRID_LRA_CACHED)
+    if not pairs or t_iter_ms <= 0:
+        return None
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clock_info or {}).get("sm_mhz") or (clock_info or {}).get("sm_max_mhz") or 2070.0
+    peak = sms * 128 * mhz * 1e6 / 1e12
+    ach = pairs * LRA_OPS_PER_PAIR / (t_iter_ms / 1000.0) / 1e12
+    return {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s (unfused FP32 operations)",
+            "frac": ach / peak, "pairs_per_iteration": pairs, "ops_per_pair": LRA_OPS_PER_PAIR,
+            "peak_source": f"{sms} SMs x 128 FP32 lanes x {mhz:.0f} MHz (nominal issue rate at the sampled clock)",
+            "note": "iteration time includes the stretch and bending work of the same launch"}
+
+
 def frame_bytes(wl, k_mean: float, interleaved_hash: int = 3) -> float:
     """Algorithmic bytes of one frame over every cloth (compulsory traffic, vec3 = 12 B,
     index = 4 B, each datum once per kernel phase): per substep predict 48 + SDF 36 +
@@ -718,6 +745,9 @@ def main() -> None:
                     "algorithmic_bytes_per_launch": iteration_bytes(wl),
                     "avg_iteration_ms": t_iter_ms, "peak_source": f"{peak_kind} hbm_gbs",
                     "stage_ms_per_frame": {k: round(v[1] / 2, 4) for k, v in prof.items()}}
+        lra = lra_fp32_roofline(wl, t_iter_ms, clock_info)
+        if lra is not None:
+            roofline["lra_fp32"] = lra
 
     # ---- end to end through the C ABI: colliders from host memory every frame, all
     # positions + normals read back into pinned host memory every frame.  Synchronous

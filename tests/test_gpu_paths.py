@@ -136,6 +136,25 @@ def test_many_lra_slots_recompute_their_rests(n_slots, variant):
         vg.lib().vt_tuning_set_grid_tile(-1)
 
 
+@pytest.mark.parametrize("n_slots", [2, 24])
+def test_lra_at_stretchiness_one_keeps_every_boundary_pair_exact(n_slots):
+    """Long-range stretchiness 1.0: every LRA pair starts at its target distance, so the
+    squared-distance filter that lets a pair skip its square roots sees pairs on both
+    sides of its bound and just inside it for the whole run; the cached (2 slots) and
+    recomputed (24 slots) forms must stay bit-exact with the oracle."""
+    side = 24
+    attached = [0, side - 1] if n_slots == 2 else list(range(0, side, side // n_slots))[:n_slots]
+    spec = spec_of(side, 0.4, attached=attached)
+    p = vg.default_params()
+    p.long_range_stretchiness = 1.0
+    o, g = Oracle(params=p), vg.ClothSolver(p)
+    for s in (o, g):
+        W.build_plain(spec, s)
+    run_frames([o, g], spec, 6)
+    same(g.positions(), o.positions(), f"{n_slots} LRA slots at stretchiness 1")
+    same(g.velocities(), o.velocities(), f"{n_slots} LRA slots at stretchiness 1, velocities")
+
+
 def checkerboard_mesh(res, size):
     """A grid whose quad diagonals alternate direction: not the reference's mesh."""
     verts, _ = W.grid_mesh(res, size)

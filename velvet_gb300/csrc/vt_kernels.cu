@@ -295,6 +295,52 @@ __device__ __forceinline__ void attach_one(vec3 pi, float wi, vec3 slot, float t
     }
 }
 
+// Filters that let an attachment which cannot fire skip its square roots.  They rest on
+// two facts: a correctly rounded sqrt is monotone, so sqrt(q) < t (t a float) gives
+// RN(sqrt(q)) <= t and the test d > t fails; and each rounding moves a product by at most
+// a factor (1 +- 2^-24).  kAttachMargin = 1 - 2^-20 (exact in FP32) absorbs those factors
+// with room to spare; the range guards keep every bound a normal, finite number (no
+// underflow, where the relative error of a product is unbounded).  Pairs the filter does
+// not drop take the exact path, so results and their order are attach_one's.
+constexpr float kAttachMargin = 1.0f - 1.0f / 1048576.0f;
+
+// attach_one for a particle with wi != 0 and a known target t: skips the pair when
+// q = |pi - slot|^2 < RN(RN(t*t) * margin) <= t^2 (1+2^-24)^2 (1-2^-20) < t^2.
+__device__ __forceinline__ void attach_one_filtered(vec3 pi, float wi, vec3 slot, float target, vec3& acc,
+                                                    int& cnt)
+{
+    if (wi != 0.0f && target > 1e-18f && target < 1e18f) {
+        const vec3 diff = pi - slot;
+        const float q = dot(diff, diff);
+        if (q < (target * target) * kAttachMargin) return;
+        const float d = sqrtf(q);
+        if (d > target) {
+            acc3(acc, (-diff) + (diff / d) * target);
+            cnt++;
+        }
+        return;
+    }
+    attach_one(pi, wi, slot, target, acc, cnt);
+}
+
+// An LRA attachment whose rest distance |slot0 - x0i| is recomputed: target =
+// RN(RN(sqrt(q0)) * lrs) >= sqrt(q0) lrs (1-2^-24)^2, so with c2 = RN(RN(lrs*lrs) * margin)
+// the bound RN(q0 * c2) <= q0 lrs^2 (1+2^-24)^3 (1-2^-20) < target^2 and a pair below it
+// needs neither square root.  The guards on q0 and lrs keep lrs^2, q0 * c2 and the target
+// within the normal range.
+__device__ __forceinline__ void attach_lra_filtered(vec3 pi, float wi, vec3 slot, vec3 slot0, vec3 x0i, float lrs,
+                                                    float c2, vec3& acc, int& cnt)
+{
+    const vec3 r = slot0 - x0i;
+    const float q0 = dot(r, r);
+    if (wi != 0.0f && q0 > 1e-20f && q0 < 1e20f && lrs > 1e-4f && lrs < 1e4f) {
+        const vec3 diff = pi - slot;
+        const float q = dot(diff, diff);
+        if (q < q0 * c2) return;
+    }
+    attach_one(pi, wi, slot, sqrtf(q0) * lrs, acc, cnt);
+}
+
 // ApplyDeltas (VtClothSolverGPU.cu:253-264) and, by mode, Finalize (:388-407) and the
 // next substep's PredictPositions (:42-53); writes x, v, p_out of particle i.  `xsrc`
 // holds x[i] (global memory, or a shared-memory copy staged by the caller).
@@ -500,20 +546,19 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
     if (a < R) VT_TAKE(sst[1][gx][gy], nw);                     // t1, first endpoint
     if (a < R && b < R) VT_TAKE(sst[2][gx][gy], nw);            // t2, first endpoint
 #undef VT_TAKE
-    // long-range attachments, slot order
+    // long-range attachments, slot order; pairs that cannot fire skip their square roots
     if (ns) {
         if (ns <= kGridLraCached) {
             const float4 r4 = *gl;
             const float rs[4] = {r4.x, r4.y, r4.z, r4.w};
 #pragma unroll
             for (int k = 0; k < kGridLraCached; ++k)
-                if (k < ns) attach_one(pi, wi, xyz(sslot[k]), rs[k] * lrs, acc, cnt);
+                if (k < ns) attach_one_filtered(pi, wi, xyz(sslot[k]), rs[k] * lrs, acc, cnt);
         } else {
             const vec3 x0i = xyz(x0[i]);
-            for (int s = s0; s < s0 + ns; ++s) {
-                const float rest = length(xyz(slots0[s]) - x0i);
-                attach_one(pi, wi, xyz(slots[s]), rest * lrs, acc, cnt);
-            }
+            const float c2 = (lrs * lrs) * kAttachMargin;
+            for (int s = s0; s < s0 + ns; ++s)
+                attach_lra_filtered(pi, wi, xyz(slots[s]), xyz(slots0[s]), x0i, lrs, c2, acc, cnt);
         }
     }
     // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
