@@ -50,6 +50,12 @@ __device__ __forceinline__ void cp_async_wait_all()
 // ------------------------------------------------------------------ colliders
 __device__ __forceinline__ float sgnf(float v) { return (v > 0) ? 1.0f : (v < 0 ? -1.0f : 0.0f); }
 
+// 1 + 2^-20 (exact in FP32): with it RN(RN(r*r) * kFarMargin) >= r^2 (1-2^-24)^2 (1+2^-20)
+// > r^2 for r^2 in the normal range, so a squared distance at or above that bound has a
+// correctly rounded square root >= r: the distance test `d >= r` can be decided without
+// taking the root (the root is monotone and r is a float).
+constexpr float kFarMargin = 1.0f + 1.0f / 1048576.0f;
+
 // SDFCollider::ComputeSDF, Velvet/VtClothSolverGPU.cuh:22-89
 __device__ vec3 collider_sdf(const ColliderDev& c, vec3 t, float margin)
 {
@@ -59,7 +65,11 @@ __device__ vec3 collider_sdf(const ColliderDev& c, vec3 t, float margin)
     } else if (c.type == 0) {  // sphere
         float radius = c.sx + margin;
         vec3 diff = t - mk3(c.px, c.py, c.pz);
-        float distance = length(diff);
+        const float q = dot(diff, diff);
+        // outside for sure (no square root): q >= RN(RN(r*r) * (1 + 2^-20)) > r^2 gives
+        // RN(sqrt(q)) >= r, so offset >= 0, whatever the rounding (r kept in the normal range)
+        if (radius > 1e-18f && radius < 1e18f && q >= (radius * radius) * kFarMargin) return mk3(0, 0, 0);
+        float distance = sqrtf(q);
         float offset = distance - radius;
         if (offset < 0) {
             vec3 direction = diff / distance;
@@ -191,6 +201,8 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
         const uint32_t* nb = nbr + D.nbr_base + (i - D.p_begin);
         const int stride = D.p_count;
         const float diam = D.diameter;
+        const bool far_ok = diam > 1e-18f && diam < 1e18f;
+        const float far2 = (diam * diam) * kFarMargin;
         // the next list entry is requested while this one is processed
         uint32_t jn = __ldg(nb);
         for (int k = 0; k < D.max_nbr; ++k) {
@@ -203,7 +215,9 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
             if (denom <= 0) continue;
             const vec3 pj = xyz(pj4);
             const vec3 diff = pi - pj;
-            const float d = length(diff);
+            const float q = dot(diff, diff);
+            if (far_ok && q >= far2) continue;  // d >= diam without the square root
+            const float d = sqrtf(q);
             if (d >= diam) continue;
             const vec3 grad = diff / (d + VT_EPSILON);
             const float lambda = (d - diam) / denom;
@@ -474,11 +488,66 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
 // evaluated once at registration with the same FP32 operations instead of every
 // iteration: the kernels are bound by instruction issue, HBM is mostly idle.
 
+// stretch_common on a difference diff = pa - pb and its length d computed by the caller.
+__device__ __forceinline__ bool stretch_common_d(vec3 diff, float d, float wa, float wb, float rest, vec3& common)
+{
+    const float denom = wa + wb;
+    if (!(d != rest && denom > 0)) return false;
+    const vec3 grad = diff / (d + VT_EPSILON);
+    const float lambda = (d - rest) / denom;
+    common = grad * lambda;
+    return true;
+}
+
+// bend_eval for the quad of a grid generator, p0 = (x,y), p1 = (x+1,y+1), p2 = (x,y+1),
+// p3 = (x+1,y), given d3 = |p2 - p3|, the length the generator's stretch constraint t3
+// already took: the shared edge e = p3 - p2 is its exact negation, so |e| = d3 bit for bit
+// and its square root is not taken again.  Every other operation is bend_eval's, in its
+// order, so the corrections are bend_eval's bits.
+__device__ __forceinline__ void bend_eval_grid(float4 a0, float4 a1, float4 a2, float4 a3, float d3, float rest,
+                                               float xpbd, float4& c0, float4& c1, float4& c2, float4& c3)
+{
+    const vec3 p0 = xyz(a0), p1 = xyz(a1), p2 = xyz(a2), p3 = xyz(a3);
+    const float w0 = a0.w, w1 = a1.w, w2 = a2.w, w3 = a3.w;
+    c0 = make_float4(0, 0, 0, 0);
+    c1 = c0;
+    c2 = c0;
+    c3 = c0;
+    const vec3 e = p3 - p2;
+    const float elen = d3;
+    if (elen < VT_EPSILON) return;
+    const float inv = 1.0f / elen;
+    vec3 n1 = cross(p2 - p0, p3 - p0);
+    n1 = n1 / dot(n1, n1);
+    vec3 n2 = cross(p3 - p1, p2 - p1);
+    n2 = n2 / dot(n2, n2);
+    const vec3 d0 = n1 * elen;
+    const vec3 d1 = n2 * elen;
+    const vec3 d2 = n1 * (dot(p0 - p3, e) * inv) + n2 * (dot(p1 - p3, e) * inv);
+    const vec3 dd3 = n1 * (dot(p2 - p0, e) * inv) + n2 * (dot(p2 - p1, e) * inv);
+    n1 = normalize(n1);
+    n2 = normalize(n2);
+    const float phi = vt_acosf(gclamp(dot(n1, n2), -1.0f, 1.0f));
+    float lambda = w0 * dot(d0, d0) + w1 * dot(d1, d1);
+    lambda = lambda + w2 * dot(d2, d2);
+    lambda = lambda + w3 * dot(dd3, dd3);
+    if (lambda < VT_EPSILON) return;
+    lambda = (phi - rest) / (lambda + xpbd);
+    if (dot(cross(n1, n2), e) > 0.0f) lambda = -lambda;
+    const vec3 k0 = d0 * (-w0 * lambda), k1 = d1 * (-w1 * lambda);
+    const vec3 k2 = d2 * (-w2 * lambda), k3 = dd3 * (-w3 * lambda);
+    c0 = make_float4(k0.x, k0.y, k0.z, 1.0f);
+    c1 = make_float4(k1.x, k1.y, k1.z, 1.0f);
+    c2 = make_float4(k2.x, k2.y, k2.z, 1.0f);
+    c3 = make_float4(k3.x, k3.y, k3.z, 1.0f);
+}
+
 // Generator (X, Y) of a grid cloth of R x R quads: its stretch constraints t0..t3 (rests
 // rest.x .. rest.w) and the bend of quad (X, Y), from the predicted position of (X, Y) at
 // sp[hx][hy] and of (X,Y+1), (X+1,Y), (X+1,Y+1) beside it.  Each stretch result goes to
 // sst[t][gx][gy] (lambda * gradient, w = 1 when it fired) and each bending corner to
-// sbd[c][gx][gy] as soon as it is known; a generator outside the cloth writes zeros.
+// sbd[c][gx][gy]; a generator outside the cloth writes zeros.  The bend reuses t3's
+// length (bend_eval_grid).
 template <int kHB, int kGA, int kGB>
 __device__ __forceinline__ void grid_generator(int X, int Y, int R, const float4 (*sp)[kHB], int hx, int hy,
                                                float4 (*sst)[kGA][kGB], float4 (*sbd)[kGA][kGB], int gx,
@@ -502,12 +571,17 @@ __device__ __forceinline__ void grid_generator(int X, int Y, int R, const float4
         r = make_float4(cm.x, cm.y, cm.z, 1.0f);
     sst[2][gx][gy] = r;
     r = zero;
-    if (full && stretch_common(sp[hx][hy + 1], sp[hx + 1][hy], rest.w, cm))  // t3: (x,y+1)-(x+1,y)
-        r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+    float d3 = 0.0f;
+    if (full) {  // t3: (x,y+1)-(x+1,y); its length is the bend's shared-edge length
+        const float4 a01 = sp[hx][hy + 1], a10 = sp[hx + 1][hy];
+        const vec3 e3 = xyz(a01) - xyz(a10);
+        d3 = length(e3);
+        if (stretch_common_d(e3, d3, a01.w, a10.w, rest.w, cm)) r = make_float4(cm.x, cm.y, cm.z, 1.0f);
+    }
     sst[3][gx][gy] = r;
     float4 c0 = zero, c1 = zero, c2 = zero, c3 = zero;
     if (full)  // bend of quad (x, y): corners (x,y), (x+1,y+1), (x,y+1), (x+1,y)
-        bend_eval(pxy, sp[hx + 1][hy + 1], sp[hx][hy + 1], sp[hx + 1][hy], 0.0f, xpbd, c0, c1, c2, c3);
+        bend_eval_grid(pxy, sp[hx + 1][hy + 1], sp[hx][hy + 1], sp[hx + 1][hy], d3, 0.0f, xpbd, c0, c1, c2, c3);
     sbd[0][gx][gy] = c0;
     sbd[1][gx][gy] = c1;
     sbd[2][gx][gy] = c2;
