@@ -749,12 +749,17 @@ def main() -> None:
         if lra is not None:
             roofline["lra_fp32"] = lra
 
+    grid_tile = vg.grid_variant_name(batch.grid_tile())
+    batch.close()
+
     # ---- end to end through the C ABI: colliders from host memory every frame, all
     # positions + normals read back into pinned host memory every frame.  Synchronous
     # form: each step waits for its own read-back.  Pipelined form (the headline): frame
     # k+1 is enqueued while frame k's read-back copies run on a second stream, the host
     # waits for frame k's copies before enqueuing frame k+2, and every copy completes
-    # inside the timed region.
+    # inside the timed region.  Each form runs on a freshly built batch over the same
+    # frames as the device-resident loop (the cost of a frame changes as the cloths fall
+    # onto their colliders), so the forms differ only in how the host drives them.
     host_pos = [torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
     host_nrm = [torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
     sh = vg.stream_handle(stream)
@@ -762,44 +767,55 @@ def main() -> None:
     ch = vg.stream_handle(copy_stream)
     copied = [torch.cuda.Event(), torch.cuda.Event()]
 
-    def e2e_step(f):
-        batch_frame(wl, batch, f, stream, upload_colliders=True)
-        _abi.check(vg.lib().vt_batch_all_get(batch.handle, 0, host_pos[0].data_ptr(), 1, sh), "all_get")
-        _abi.check(vg.lib().vt_batch_all_get(batch.handle, 1, host_nrm[0].data_ptr(), 1, sh), "all_get")
+    def e2e_step(b, f):
+        batch_frame(wl, b, f, stream, upload_colliders=True)
+        _abi.check(vg.lib().vt_batch_all_get(b.handle, 0, host_pos[0].data_ptr(), 1, sh), "all_get")
+        _abi.check(vg.lib().vt_batch_all_get(b.handle, 1, host_nrm[0].data_ptr(), 1, sh), "all_get")
         stream.synchronize()
 
-    def e2e_pipelined(f):
-        batch_frame(wl, batch, f, stream, upload_colliders=True)
-        _abi.check(vg.lib().vt_batch_all_get_async(batch.handle, 0, host_pos[f % 2].data_ptr(), ch), "all_get_async")
-        _abi.check(vg.lib().vt_batch_all_get_async(batch.handle, 1, host_nrm[f % 2].data_ptr(), ch), "all_get_async")
+    host_enqueue_s = [0.0]
+
+    def e2e_pipelined(b, f):
+        t = time.perf_counter()
+        batch_frame(wl, b, f, stream, upload_colliders=True)
+        _abi.check(vg.lib().vt_batch_all_get_async(b.handle, 0, host_pos[f % 2].data_ptr(), ch), "all_get_async")
+        _abi.check(vg.lib().vt_batch_all_get_async(b.handle, 1, host_nrm[f % 2].data_ptr(), ch), "all_get_async")
         copied[f % 2].record(copy_stream)
+        host_enqueue_s[0] += time.perf_counter() - t
         if f > 0:
             copied[(f - 1) % 2].synchronize()  # frame f-1 is in host memory
 
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = args.steps
+    batch = build_batch(wl)
     for f in range(args.warmup):
-        e2e_step(f)
+        e2e_step(batch, f)
     dist_sync()
     t0 = time.perf_counter()
     for k in range(e2e_steps):
-        e2e_step(k)
+        e2e_step(batch, args.warmup + k)
     e2e_sync_s = max_over_ranks(time.perf_counter() - t0)
+    batch.close()
+    batch = build_batch(wl)
     for f in range(args.warmup):
-        e2e_pipelined(f)
+        e2e_pipelined(batch, f)
     copy_stream.synchronize()
     dist_sync()
+    host_enqueue_s[0] = 0.0
+    e_first, e_last = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
+    e_first.record(stream)
     for k in range(e2e_steps):
-        e2e_pipelined(k)
+        e2e_pipelined(batch, args.warmup + k)
+    e_last.record(stream)
     copy_stream.synchronize()
     stream.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_device_ms = e_first.elapsed_time(e_last) / e2e_steps
     e2e_value = job_pits * e2e_steps / e2e_s
     e2e_sync_value = job_pits * e2e_steps / e2e_sync_s
     ncol = sum(len(c.colliders(0)) for c in wl.cloths)
     h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
     d2h = n_tot * 24
-    grid_tile = vg.grid_variant_name(batch.grid_tile())
     batch.close()
 
     # ---- the plain drop-in solver on the same workload, one cloth at a time
@@ -848,7 +864,10 @@ def main() -> None:
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "mode": "pipelined: frame k+1 computes while frame k's positions and normals copy to pinned "
                             "host memory (vt_batch_all_get_async); all copies inside the timed region",
-                    "synchronous_value": e2e_sync_value},
+                    "synchronous_value": e2e_sync_value, "steps": e2e_steps,
+                    "wall_ms_per_frame": 1000.0 * e2e_s / e2e_steps,
+                    "device_ms_per_frame": e2e_device_ms,
+                    "host_enqueue_ms_per_frame": 1000.0 * host_enqueue_s[0] / e2e_steps},
             "gpu_launches": launches_timed,
             "roofline": roofline,
             "cpu_baseline": cpu,

@@ -631,6 +631,8 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
         } else {
             const vec3 x0i = xyz(x0[i]);
             const float c2 = (lrs * lrs) * kAttachMargin;
+            // unrolled: the next slots' loads overlap this pair's arithmetic
+#pragma unroll 4
             for (int s = s0; s < s0 + ns; ++s)
                 attach_lra_filtered(pi, wi, xyz(slots[s]), xyz(slots0[s]), x0i, lrs, c2, acc, cnt);
         }
