@@ -155,6 +155,24 @@ def test_lra_at_stretchiness_one_keeps_every_boundary_pair_exact(n_slots):
     same(g.velocities(), o.velocities(), f"{n_slots} LRA slots at stretchiness 1, velocities")
 
 
+@pytest.mark.parametrize("lrs", [1.2, 1.0])
+@pytest.mark.parametrize("side,rows", [(64, 1), (40, 30)])
+def test_lra_slot_groups_skip_only_quiet_groups(side, rows, lrs):
+    """Whole attached rows (64 slots: four groups of 16; 1,200 slots: 64 groups of 19, the
+    last of 3): the tile kernel skips a group of slots when bounding boxes prove none of
+    its pairs fires.  Stretchiness 1.0 puts pairs at their bound; the result must be the
+    oracle's."""
+    spec = spec_of(side, 0.4, attached=list(range(rows * side)))
+    p = vg.default_params()
+    p.long_range_stretchiness = lrs
+    o, g = Oracle(params=p), vg.ClothSolver(p)
+    for s in (o, g):
+        W.build_plain(spec, s)
+    run_frames([o, g], spec, 3 if rows > 1 else 6)
+    same(g.positions(), o.positions(), f"{rows * side} slots, stretchiness {lrs}")
+    same(g.velocities(), o.velocities(), f"{rows * side} slots, stretchiness {lrs}, velocities")
+
+
 def checkerboard_mesh(res, size):
     """A grid whose quad diagonals alternate direction: not the reference's mesh."""
     verts, _ = W.grid_mesh(res, size)

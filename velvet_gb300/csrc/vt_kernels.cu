@@ -355,6 +355,93 @@ __device__ __forceinline__ void attach_lra_filtered(vec3 pi, float wi, vec3 slot
     attach_one(pi, wi, slot, sqrtf(q0) * lrs, acc, cnt);
 }
 
+// Groups of LRA slots (cloths with more slots than the per-particle cache): a whole group
+// is skipped when bounds prove that every one of its pairs passes attach_lra_filtered's
+// test q < RN(q0 * c2), so that none fires.  Per group, boxes [lo, hi] of the current and
+// [lo0, hi0] of the rest slot positions (w of lo = 1 when a coordinate of the group is
+// non-finite or beyond 1e9: never skipped).  With u = 2^-24, for every slot s of the group:
+//  * D = per-axis max(|p - lo|, |p - hi|) (rounded differences are >= the real ones times
+//    1 - u) bounds |p - slot_s| per axis; the computed q_s <= |D|^2 (1+u)^5/(1-u)^5, and
+//    qu = RN(RN(|D|^2) * (1 + 2^-18)) is above that;
+//  * E = per-axis distance from x0 to the rest box bounds |slot0_s - x0| per axis from
+//    below; the computed q0_s >= |E|^2 (1-u)^5/(1+u)^5, and ql = RN(RN(|E|^2) * (1 - 2^-18))
+//    is below that;
+//  * then RN(RN(ql * c2) * (1 - 2^-18)) <= ql c2 (1+u)^2 (1 - 2^-18) < q0_s c2 (1 - u) <=
+//    RN(q0_s * c2), so qu below it gives q_s < RN(q0_s * c2) for the whole group.
+// Coordinates below 1e9 keep q0_s < 1e20 and every product finite; |D|^2, |E|^2 > 1e-20
+// keep the absolute error of an underflowed component square (<= 2^-149 each) far inside
+// the margins; q0_s >= ql > 1e-20 meets attach_lra_filtered's own guard.
+constexpr int kLraGroupMin = 16;      // slots per group (more when a cloth has > 1024)
+constexpr int kLraGroupsMax = 64;     // groups per cloth: 4 boxes each fill kBlock float4
+static_assert(4 * kLraGroupsMax <= kBlock && kLraGroupsMax * 4 == kBlock, "group boxes fill the LRA rest array");
+constexpr float kBoundUp = 1.0f + 1.0f / 262144.0f;
+constexpr float kBoundDown = 1.0f - 1.0f / 262144.0f;
+
+__device__ __forceinline__ bool in_bound_range(vec3 v)
+{
+    return fabsf(v.x) < 1e9f && fabsf(v.y) < 1e9f && fabsf(v.z) < 1e9f;
+}
+
+// The four boxes of each group of the domain's ns slots, into box[4 g .. 4 g + 3]; four
+// threads per group (all threads of the block take part in the warp shuffles).
+__device__ __forceinline__ void lra_group_boxes(float4* box, const float4* __restrict__ slots,
+                                                const float4* __restrict__ slots0, int ns, int gsize,
+                                                int ngroups, int tid)
+{
+    const int g = tid >> 2, q = tid & 3;
+    const float inf = __int_as_float(0x7f800000);
+    vec3 lo = mk3(inf, inf, inf), hi = mk3(-inf, -inf, -inf), lo0 = lo, hi0 = hi;
+    int bad = 0;
+    if (g < ngroups) {
+        const int sb = g * gsize, se = min(sb + gsize, ns);
+        for (int s = sb + q; s < se; s += 4) {
+            const vec3 a = xyz(slots[s]), b = xyz(slots0[s]);
+            bad |= (in_bound_range(a) && in_bound_range(b)) ? 0 : 1;
+            lo = mk3(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z));
+            hi = mk3(fmaxf(hi.x, a.x), fmaxf(hi.y, a.y), fmaxf(hi.z, a.z));
+            lo0 = mk3(fminf(lo0.x, b.x), fminf(lo0.y, b.y), fminf(lo0.z, b.z));
+            hi0 = mk3(fmaxf(hi0.x, b.x), fmaxf(hi0.y, b.y), fmaxf(hi0.z, b.z));
+        }
+    }
+#pragma unroll
+    for (int m = 1; m <= 2; m <<= 1) {
+        bad |= __shfl_xor_sync(0xffffffffu, bad, m);
+        lo = mk3(fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, m)), fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, m)),
+                 fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, m)));
+        hi = mk3(fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, m)), fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, m)),
+                 fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, m)));
+        lo0 = mk3(fminf(lo0.x, __shfl_xor_sync(0xffffffffu, lo0.x, m)),
+                  fminf(lo0.y, __shfl_xor_sync(0xffffffffu, lo0.y, m)),
+                  fminf(lo0.z, __shfl_xor_sync(0xffffffffu, lo0.z, m)));
+        hi0 = mk3(fmaxf(hi0.x, __shfl_xor_sync(0xffffffffu, hi0.x, m)),
+                  fmaxf(hi0.y, __shfl_xor_sync(0xffffffffu, hi0.y, m)),
+                  fmaxf(hi0.z, __shfl_xor_sync(0xffffffffu, hi0.z, m)));
+    }
+    if (g < ngroups && q == 0) {
+        box[4 * g + 0] = make_float4(lo.x, lo.y, lo.z, bad ? 1.0f : 0.0f);
+        box[4 * g + 1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+        box[4 * g + 2] = make_float4(lo0.x, lo0.y, lo0.z, 0.0f);
+        box[4 * g + 3] = make_float4(hi0.x, hi0.y, hi0.z, 0.0f);
+    }
+}
+
+// True when no pair of the group can fire for the particle at p with rest position x0
+// (the caller has checked wi != 0, lrs in (1e-4, 1e4) and p, x0 in range).
+__device__ __forceinline__ bool lra_group_quiet(vec3 p, vec3 x0, const float4* box, float c2)
+{
+    const float4 lo = box[0], hi = box[1], lo0 = box[2], hi0 = box[3];
+    if (lo.w != 0.0f) return false;
+    const vec3 D = mk3(fmaxf(fabsf(p.x - lo.x), fabsf(p.x - hi.x)), fmaxf(fabsf(p.y - lo.y), fabsf(p.y - hi.y)),
+                       fmaxf(fabsf(p.z - lo.z), fabsf(p.z - hi.z)));
+    const vec3 E = mk3(fmaxf(fmaxf(lo0.x - x0.x, x0.x - hi0.x), 0.0f), fmaxf(fmaxf(lo0.y - x0.y, x0.y - hi0.y), 0.0f),
+                       fmaxf(fmaxf(lo0.z - x0.z, x0.z - hi0.z), 0.0f));
+    const float qf = dot(D, D), q0f = dot(E, E);
+    if (!(qf > 1e-20f && q0f > 1e-20f)) return false;
+    const float qu = qf * kBoundUp, ql = q0f * kBoundDown;
+    if (!(ql > 1e-20f)) return false;
+    return qu < (ql * c2) * kBoundDown;
+}
+
 // ApplyDeltas (VtClothSolverGPU.cu:253-264) and, by mode, Finalize (:388-407) and the
 // next substep's PredictPositions (:42-53); writes x, v, p_out of particle i.  `xsrc`
 // holds x[i] (global memory, or a shared-memory copy staged by the caller).
@@ -591,13 +678,14 @@ __device__ __forceinline__ void grid_generator(int X, int Y, int R, const float4
 // The Jacobi sum of grid particle (a, b), i = its index: its eight stretch constraints,
 // its LRA attachments in slot order, its four bending corners, all in constraint order.
 // Generator (a, b)'s results sit at [gx][gy] of sst / sbd, generator (a-1, b-1)'s at
-// [gx-1][gy-1].  gl: the particle's cached LRA rest distances, sslot: the cached slots.
+// [gx-1][gy-1].  gl: the particle's cached LRA rest distances, sslot: the cached slots;
+// gbox: the slot groups' boxes (more slots than the cache holds), ngroups of gsize.
 template <int kGA, int kGB>
 __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, int gx, int gy,
                                                   const float4 (*sst)[kGA][kGB], const float4 (*sbd)[kGA][kGB],
                                                   vec3 pi, float wi, int ns, int s0, const float4* gl,
-                                                  const float4* sslot, const float4* __restrict__ x0,
-                                                  const float4* __restrict__ slots,
+                                                  const float4* sslot, const float4* gbox, int gsize, int ngroups,
+                                                  const float4* __restrict__ x0, const float4* __restrict__ slots,
                                                   const float4* __restrict__ slots0, float lrs, vec3& acc,
                                                   int& cnt)
 {
@@ -631,10 +719,15 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
         } else {
             const vec3 x0i = xyz(x0[i]);
             const float c2 = (lrs * lrs) * kAttachMargin;
-            // unrolled: the next slots' loads overlap this pair's arithmetic
+            const bool quiet_ok = wi != 0.0f && lrs > 1e-4f && lrs < 1e4f && in_bound_range(pi) && in_bound_range(x0i);
+            for (int g = 0; g < ngroups; ++g) {
+                if (quiet_ok && lra_group_quiet(pi, x0i, gbox + 4 * g, c2)) continue;  // no pair of it fires
+                const int sb = s0 + g * gsize, se = min(sb + gsize, s0 + ns);
+                // unrolled: the next slots' loads overlap this pair's arithmetic
 #pragma unroll 4
-            for (int s = s0; s < s0 + ns; ++s)
-                attach_lra_filtered(pi, wi, xyz(slots[s]), xyz(slots0[s]), x0i, lrs, c2, acc, cnt);
+                for (int s = sb; s < se; ++s)
+                    attach_lra_filtered(pi, wi, xyz(slots[s]), xyz(slots0[s]), x0i, lrs, c2, acc, cnt);
+            }
         }
     }
     // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
@@ -675,7 +768,7 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     // slot (gx * kGGB + gy == tid): the thread reads them before it writes that slot
     float4* const sgr = &sst[0][0][0];
     __shared__ float4 sbd[4][kGGA][kGGB];  // bending corner corrections + fired flag
-    __shared__ float4 sgl[kBlock];         // the particle's LRA rest distances
+    __shared__ float4 sgl[kBlock];         // the particle's LRA rest distances, or the slot groups' boxes
     __shared__ float4 sx[kBlock];          // the particle's position (finalizing modes)
     __shared__ float4 sslot[kGridLraCached];
     __shared__ __align__(16) DomainParams sdom;
@@ -714,8 +807,15 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     __syncthreads();
     const DomainParams& D = sdom;
 
-    // 2. generators (x, y) = (a0 - 1 + gx, b0 - 1 + gy): one per thread (the rests are
-    // read before sst[0][gx][gy], the same slot, is written)
+    // 2. the slot groups' boxes when the cloth has more LRA slots than the cache holds
+    // (sgl is free then), then the generators (x, y) = (a0 - 1 + gx, b0 - 1 + gy): one per
+    // thread (the rests are read before sst[0][gx][gy], the same slot, is written)
+    int gsize = 0, ngroups = 0;
+    if (ns > kGridLraCached) {
+        gsize = max(kLraGroupMin, (ns + kLraGroupsMax - 1) / kLraGroupsMax);
+        ngroups = (ns + gsize - 1) / gsize;
+        lra_group_boxes(sgl, slots + s0, slots0 + s0, ns, gsize, ngroups, tid);
+    }
     grid_generator<kGHB, kGGA, kGGB>(a0 - 1 + gx, b0 - 1 + gy, R, sp, gx, gy, sst, sbd, gx, gy, sgr[tid],
                                      D.xpbd_bend);
     __syncthreads();
@@ -729,8 +829,8 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     const float wi = pi4.w;
     vec3 acc = mk3(0, 0, 0);
     int cnt = 0;
-    grid_particle_sum<kGGA, kGGB>(a, b, R, i, hx, hy, sst, sbd, pi, wi, ns, s0, &sgl[tid], sslot, x0, slots,
-                                  slots0, D.lrs, acc, cnt);
+    grid_particle_sum<kGGA, kGGB>(a, b, R, i, hx, hy, sst, sbd, pi, wi, ns, s0, &sgl[tid], sslot, sgl, gsize,
+                                  ngroups, x0, slots, slots0, D.lrs, acc, cnt);
     apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, &sx[tid], pout, x, v, status);
 }
 
