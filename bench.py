@@ -122,8 +122,9 @@ def lra_roofline(wl, t_iter_ms: float, clock_info) -> dict | None:
             "ops_per_pair_if_evaluated": LRA_OPS_PER_PAIR, "equivalent_tflops": eq,
             "fp32_issue_peak_tflops": peak, "equivalent_over_peak": eq / peak,
             "peak_source": f"{sms} SMs x 128 FP32 lanes x {mhz:.0f} MHz (nominal issue rate at the sampled clock)",
-            "note": "groups of slots (16, more above 1,024 slots) proven quiet by bounding boxes are skipped; an equivalent rate "
-                    "above the issue peak is the work the bound removes, not an achieved rate"}
+            "note": "groups of slots (16, more above 1,024 slots) proven quiet by bounding boxes are "
+                    "skipped; an equivalent rate above the issue peak is the work the bound removes, "
+                    "not an achieved rate"}
 
 
 def frame_bytes(wl, k_mean: float, interleaved_hash: int = 3) -> float:
