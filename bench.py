@@ -162,10 +162,10 @@ def mean_cached_neighbours(solvers, max_particles: int = 400_000) -> float | Non
 
 
 # DRAM traffic of one k_grid_iter launch per particle: ncu dram__bytes_read.sum +
-# dram__bytes_write.sum = 50.57 + 3.18 MB on a 1024x1024 cloth (1,050,625 particles,
+# dram__bytes_write.sum = 50.54 + 0.76 MB on a 1024x1024 cloth (1,050,625 particles,
 # two LRA slots); the kernel reads the same float4 streams for every grid cloth, so the
 # figure scales with the particles a launch covers.
-GRID_ITER_DRAM_BYTES_PER_PARTICLE = (50.57e6 + 3.18e6) / 1050625
+GRID_ITER_DRAM_BYTES_PER_PARTICLE = (50.544e6 + 0.759e6) / 1050625
 
 
 class ClockSampler:
@@ -645,6 +645,8 @@ def main() -> None:
     ap.add_argument("--form", choices=["batched", "plain"], default="batched",
                     help="form run by --profile-frames")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--grid-tile", type=int, default=-1,
+                    help="pin a grid kernel variant (velvet_gb300.GRID_VARIANTS index); -1 = autotune")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain solver")
     ap.add_argument("--profile-frames", type=int, default=0,
@@ -663,6 +665,10 @@ def main() -> None:
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.grid_tile >= 0:
+        import velvet_gb300 as vg
+
+        vg._abi.check(vg.lib().vt_tuning_set_grid_tile(args.grid_tile), "vt_tuning_set_grid_tile")
     if args.profile_frames:
         profile_frames(args)
         return
@@ -810,6 +816,7 @@ def main() -> None:
     dist_sync()
     host_enqueue_s[0] = 0.0
     e_first, e_last = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_clocks = ClockSampler(local, pci)
     t0 = time.perf_counter()
     e_first.record(stream)
     for k in range(e2e_steps):
@@ -818,6 +825,7 @@ def main() -> None:
     copy_stream.synchronize()
     stream.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_clock_info = e2e_clocks.stop()
     e2e_device_ms = e_first.elapsed_time(e_last) / e2e_steps
     e2e_value = job_pits * e2e_steps / e2e_s
     e2e_sync_value = job_pits * e2e_steps / e2e_sync_s
@@ -875,7 +883,8 @@ def main() -> None:
                     "synchronous_value": e2e_sync_value, "steps": e2e_steps,
                     "wall_ms_per_frame": 1000.0 * e2e_s / e2e_steps,
                     "device_ms_per_frame": e2e_device_ms,
-                    "host_enqueue_ms_per_frame": 1000.0 * host_enqueue_s[0] / e2e_steps},
+                    "host_enqueue_ms_per_frame": 1000.0 * host_enqueue_s[0] / e2e_steps,
+                    "clocks": e2e_clock_info},
             "gpu_launches": launches_timed,
             "roofline": roofline,
             "cpu_baseline": cpu,

@@ -138,10 +138,12 @@ public:
     int32_t total_keys = 0, n_ptiles = 0, n_btiles = 0, nbr_words = 0;
     int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
     int32_t grid_variant = 0;  // tile shape of the grid kernel (kGridVariant index)
-    // Times every grid tile shape on this world's cloths (one Jacobi iteration each, from
-    // the current positions, into scratch buffers) and keeps the fastest; decisions are
-    // cached per size signature for the process.  Never changes a result.
-    vt_status autotune(cudaStream_t st);
+    // Times every grid kernel variant on this world's cloths (one Jacobi iteration each,
+    // from the current positions, into scratch buffers) and keeps the fastest; decisions
+    // are cached per size signature for the process.  A cached or forced variant applies
+    // at once; timing waits for may_time (a frame simulated), the default variant runs
+    // until then.  Never changes a result.
+    vt_status autotune(cudaStream_t st, bool may_time);
     vt_status set_grid_variant(int variant);
     int32_t pcur = 0;  // which of p[0], p[1] holds the latest predicted positions
     uint64_t bytes = 0;
@@ -155,6 +157,7 @@ private:
     cudaEvent_t staged_ = nullptr;
     bool cols_dirty_ = true, slots_dirty_ = true;
     bool tuned_ = false;
+    int64_t frames_ = 0;  // frames simulated since the last build
     std::vector<std::pair<int32_t, int32_t>> grid_doms_;  // (domain, resolution) of grid domains
     int32_t gtiles_cap_ = 0;
     // frame graph

@@ -171,7 +171,7 @@ vt_status profiler_read(vt_stage_time* out, uint32_t cap, uint32_t* count)
 namespace {
 std::mutex g_tune_mu;
 int g_forced_variant = -1;
-int g_last_tuned = 0;
+int g_last_tuned = kGridDefaultVariant;
 std::vector<std::pair<std::vector<int64_t>, int>> g_tune_cache;  // signature -> shape
 }  // namespace
 
@@ -253,6 +253,7 @@ void World::release()
     grid_doms_.clear();
     built_ = false;
     tuned_ = false;
+    frames_ = 0;
     bytes = 0;
 }
 
@@ -277,16 +278,21 @@ vt_status World::set_grid_variant(int variant)
     return VT_OK;
 }
 
-vt_status World::autotune(cudaStream_t st)
+vt_status World::autotune(cudaStream_t st, bool may_time)
 {
-    tuned_ = true;
-    if (grid_doms_.empty()) return VT_OK;
+    if (grid_doms_.empty()) {
+        tuned_ = true;
+        return VT_OK;
+    }
     int forced = -1;
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         forced = g_forced_variant;
     }
-    if (forced >= 0) return forced == grid_variant ? VT_OK : set_grid_variant(forced);
+    if (forced >= 0) {
+        tuned_ = true;
+        return forced == grid_variant ? VT_OK : set_grid_variant(forced);
+    }
     // signature: cloth count and total particles (log2 buckets), mean side
     int64_t parts = 0;
     for (auto& gd : grid_doms_) parts += (int64_t)(gd.second + 1) * (gd.second + 1);
@@ -299,8 +305,13 @@ vt_status World::autotune(cudaStream_t st)
         for (auto& e : g_tune_cache)
             if (e.first == sig) best = e.second;
     }
+    if (best < 0 && !may_time) return VT_OK;  // the default variant until a frame has moved the cloths
+    tuned_ = true;
     if (best < 0) {
-        // time one Jacobi iteration per shape from the current positions (x -> p[0] -> p[1])
+        // time one Jacobi iteration per variant from the current positions (x -> p[0] ->
+        // p[1]), once a frame has been simulated: at the registered rest state (x == x0)
+        // every stretch constraint has d == rest and returns early, which is not the cost
+        // of a frame
         VT_CUDA(cudaMemcpyAsync(d.p[0], d.x, 16 * (size_t)n_particles, cudaMemcpyDeviceToDevice, st), "tune copy");
         cudaEvent_t e0, e1;
         VT_CUDA(cudaEventCreate(&e0), "event");
@@ -549,7 +560,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         for (auto& gd : grid_doms_) grid_tiles_for(tmp, gd.first, hdom[gd.first], v);
         gtiles_cap_ = std::max(gtiles_cap_, (int32_t)tmp.size());
     }
-    grid_variant = grid_variant_for(0);
+    grid_variant = grid_variant_for(kGridDefaultVariant);
     for (auto& gd : grid_doms_) grid_tiles_for(gt, gd.first, hdom[gd.first], grid_variant);
     n_ptiles = (int32_t)pt.size();
     n_btiles = (int32_t)bt.size();
@@ -640,6 +651,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     }
     VT_CUDA(prepare_kernels(), "kernel attributes");
     tuned_ = false;
+    frames_ = 0;
     VT_CUDA(cudaMemset(d.status, 0, (1 + n_domains) * 4), "memset status");
 
     staging_bytes_ = sizeof(DomainParams) * n_domains + sizeof(ColliderDev) * C + 16 * SL + 64;
@@ -748,9 +760,10 @@ vt_status World::simulate(const FrameArgs& a, int32_t ih, bool any_self, cudaStr
     vt_status r = upload_frame(st);
     if (r != VT_OK) return r;
     if (!tuned_) {
-        r = autotune(st);
+        r = autotune(st, frames_ > 0);
         if (r != VT_OK) return r;
     }
+    ++frames_;
     if (!use_graph || profiler_on()) return enqueue_frame(a, ih, any_self, st);
     const int32_t key[4] = {a.substeps, a.iterations, ih, any_self ? 1 : 0};
     if (!gexec_ || std::memcmp(key, gkey_, sizeof(key)) != 0) {

@@ -100,6 +100,7 @@ struct GridVariant {
     int ta, tb, blocks;
 };
 constexpr int kGridVariants = 6;
+constexpr int kGridDefaultVariant = 1;  // 15x15 at four blocks: the variant used before tuning
 constexpr GridVariant kGridVariant[kGridVariants] = {{7, 31, 4}, {15, 15, 4}, {3, 63, 4},
                                                      {7, 31, 5}, {15, 15, 5}, {3, 63, 5}};
 // Tiles of variant `variant` covering the (grid_res+1)^2 grid cloth of domain `dom`.
