@@ -137,7 +137,7 @@ public:
     int32_t n_domains = 0, n_particles = 0, n_bends = 0, n_slots = 0, n_cols = 0;
     int32_t total_keys = 0, n_ptiles = 0, n_btiles = 0, nbr_words = 0;
     int32_t n_stiles = 0, n_gtiles = 0, n_gptiles = 0;
-    int32_t grid_variant = 0;  // tile shape of the grid kernel (kGridVariant index)
+    int32_t grid_variant = 0;  // grid kernel variant (kGridVariant index)
     // Times every grid kernel variant on this world's cloths (one Jacobi iteration each,
     // from the current positions, into scratch buffers) and keeps the fastest; decisions
     // are cached per size signature for the process.  A cached or forced variant applies
@@ -189,11 +189,11 @@ vt_status render_to(const float4* x, int64_t n, const vt_render_params& rp, uint
 
 ColliderDev collider_to_device(const vt_sdf_collider& c);
 
-// Grid tile shape to use: the forced one (vt_tuning_set), else `tuned`.
+// Grid kernel variant to use: the forced one (vt_tuning_set), else `tuned`.
 int grid_variant_for(int tuned);
 // Last autotuned shape in this process (0 if none), for worlds that do not tune.
 int last_tuned_variant();
-// Forces a grid tile shape for every world (-1: autotune again).
+// Forces a grid kernel variant for every world (-1: autotune again).
 vt_status tuning_force(int32_t variant);
 
 // Per-frame fields of a domain's parameter block from its vt_params and frame arguments.
