@@ -373,6 +373,7 @@ __device__ __forceinline__ void attach_lra_filtered(vec3 pi, float wi, vec3 slot
 // the margins; q0_s >= ql > 1e-20 meets attach_lra_filtered's own guard.
 constexpr int kLraGroupMin = 16;      // slots per group (more when a cloth has > 1024)
 constexpr int kLraGroupsMax = 64;     // groups per cloth: 4 boxes each fill kBlock float4
+constexpr int kLraSuper = 4;          // groups per super-group: 16 threads reduce one
 static_assert(4 * kLraGroupsMax <= kBlock && kLraGroupsMax * 4 == kBlock, "group boxes fill the LRA rest array");
 constexpr float kBoundUp = 1.0f + 1.0f / 262144.0f;
 constexpr float kBoundDown = 1.0f - 1.0f / 262144.0f;
@@ -382,9 +383,11 @@ __device__ __forceinline__ bool in_bound_range(vec3 v)
     return fabsf(v.x) < 1e9f && fabsf(v.y) < 1e9f && fabsf(v.z) < 1e9f;
 }
 
-// The four boxes of each group of the domain's ns slots, into box[4 g .. 4 g + 3]; four
-// threads per group (all threads of the block take part in the warp shuffles).
-__device__ __forceinline__ void lra_group_boxes(float4* box, const float4* __restrict__ slots,
+// The four boxes of each group of the domain's ns slots, into box[4 g .. 4 g + 3], and of
+// each super-group (kLraSuper consecutive groups) into sup[4 G .. 4 G + 3]; four threads
+// per group, sixteen per super-group (all threads of the block take part in the warp
+// shuffles).
+__device__ __forceinline__ void lra_group_boxes(float4* box, float4* sup, const float4* __restrict__ slots,
                                                 const float4* __restrict__ slots0, int ns, int gsize,
                                                 int ngroups, int tid)
 {
@@ -403,26 +406,30 @@ __device__ __forceinline__ void lra_group_boxes(float4* box, const float4* __res
             hi0 = mk3(fmaxf(hi0.x, b.x), fmaxf(hi0.y, b.y), fmaxf(hi0.z, b.z));
         }
     }
-#pragma unroll
-    for (int m = 1; m <= 2; m <<= 1) {
-        bad |= __shfl_xor_sync(0xffffffffu, bad, m);
-        lo = mk3(fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, m)), fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, m)),
-                 fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, m)));
-        hi = mk3(fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, m)), fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, m)),
-                 fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, m)));
-        lo0 = mk3(fminf(lo0.x, __shfl_xor_sync(0xffffffffu, lo0.x, m)),
-                  fminf(lo0.y, __shfl_xor_sync(0xffffffffu, lo0.y, m)),
-                  fminf(lo0.z, __shfl_xor_sync(0xffffffffu, lo0.z, m)));
-        hi0 = mk3(fmaxf(hi0.x, __shfl_xor_sync(0xffffffffu, hi0.x, m)),
-                  fmaxf(hi0.y, __shfl_xor_sync(0xffffffffu, hi0.y, m)),
-                  fmaxf(hi0.z, __shfl_xor_sync(0xffffffffu, hi0.z, m)));
-    }
-    if (g < ngroups && q == 0) {
-        box[4 * g + 0] = make_float4(lo.x, lo.y, lo.z, bad ? 1.0f : 0.0f);
-        box[4 * g + 1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
-        box[4 * g + 2] = make_float4(lo0.x, lo0.y, lo0.z, 0.0f);
-        box[4 * g + 3] = make_float4(hi0.x, hi0.y, hi0.z, 0.0f);
-    }
+    auto merge = [&](int m) {
+        const unsigned all = 0xffffffffu;
+        bad |= __shfl_xor_sync(all, bad, m);
+        lo = mk3(fminf(lo.x, __shfl_xor_sync(all, lo.x, m)), fminf(lo.y, __shfl_xor_sync(all, lo.y, m)),
+                 fminf(lo.z, __shfl_xor_sync(all, lo.z, m)));
+        hi = mk3(fmaxf(hi.x, __shfl_xor_sync(all, hi.x, m)), fmaxf(hi.y, __shfl_xor_sync(all, hi.y, m)),
+                 fmaxf(hi.z, __shfl_xor_sync(all, hi.z, m)));
+        lo0 = mk3(fminf(lo0.x, __shfl_xor_sync(all, lo0.x, m)), fminf(lo0.y, __shfl_xor_sync(all, lo0.y, m)),
+                  fminf(lo0.z, __shfl_xor_sync(all, lo0.z, m)));
+        hi0 = mk3(fmaxf(hi0.x, __shfl_xor_sync(all, hi0.x, m)), fmaxf(hi0.y, __shfl_xor_sync(all, hi0.y, m)),
+                  fmaxf(hi0.z, __shfl_xor_sync(all, hi0.z, m)));
+    };
+    auto store = [&](float4* b) {
+        b[0] = make_float4(lo.x, lo.y, lo.z, bad ? 1.0f : 0.0f);
+        b[1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+        b[2] = make_float4(lo0.x, lo0.y, lo0.z, 0.0f);
+        b[3] = make_float4(hi0.x, hi0.y, hi0.z, 0.0f);
+    };
+    merge(1);
+    merge(2);
+    if (g < ngroups && q == 0) store(box + 4 * g);
+    merge(4);
+    merge(8);
+    if ((tid & 15) == 0 && g < ngroups) store(sup + 4 * (g / kLraSuper));
 }
 
 // True when no pair of the group can fire for the particle at p with rest position x0
@@ -679,12 +686,14 @@ __device__ __forceinline__ void grid_generator(int X, int Y, int R, const float4
 // its LRA attachments in slot order, its four bending corners, all in constraint order.
 // Generator (a, b)'s results sit at [gx][gy] of sst / sbd, generator (a-1, b-1)'s at
 // [gx-1][gy-1].  gl: the particle's cached LRA rest distances, sslot: the cached slots;
-// gbox: the slot groups' boxes (more slots than the cache holds), ngroups of gsize.
+// gbox / gsup: the slot groups' and super-groups' boxes (more slots than the cache holds),
+// ngroups of gsize.
 template <int kGA, int kGB>
 __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, int gx, int gy,
                                                   const float4 (*sst)[kGA][kGB], const float4 (*sbd)[kGA][kGB],
                                                   vec3 pi, float wi, int ns, int s0, const float4* gl,
-                                                  const float4* sslot, const float4* gbox, int gsize, int ngroups,
+                                                  const float4* sslot, const float4* gbox, const float4* gsup,
+                                                  int gsize, int ngroups,
                                                   const float4* __restrict__ x0, const float4* __restrict__ slots,
                                                   const float4* __restrict__ slots0, float lrs, vec3& acc,
                                                   int& cnt)
@@ -720,13 +729,17 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
             const vec3 x0i = xyz(x0[i]);
             const float c2 = (lrs * lrs) * kAttachMargin;
             const bool quiet_ok = wi != 0.0f && lrs > 1e-4f && lrs < 1e4f && in_bound_range(pi) && in_bound_range(x0i);
-            for (int g = 0; g < ngroups; ++g) {
-                if (quiet_ok && lra_group_quiet(pi, x0i, gbox + 4 * g, c2)) continue;  // no pair of it fires
-                const int sb = s0 + g * gsize, se = min(sb + gsize, s0 + ns);
-                // unrolled: the next slots' loads overlap this pair's arithmetic
+            for (int g0 = 0; g0 < ngroups; g0 += kLraSuper) {
+                // a super-group, then each of its groups, skipped when no pair of it fires
+                if (quiet_ok && lra_group_quiet(pi, x0i, gsup + 4 * (g0 / kLraSuper), c2)) continue;
+                for (int g = g0; g < min(g0 + kLraSuper, ngroups); ++g) {
+                    if (quiet_ok && lra_group_quiet(pi, x0i, gbox + 4 * g, c2)) continue;
+                    const int sb = s0 + g * gsize, se = min(sb + gsize, s0 + ns);
+                    // unrolled: the next slots' loads overlap this pair's arithmetic
 #pragma unroll 4
-                for (int s = sb; s < se; ++s)
-                    attach_lra_filtered(pi, wi, xyz(slots[s]), xyz(slots0[s]), x0i, lrs, c2, acc, cnt);
+                    for (int s = sb; s < se; ++s)
+                        attach_lra_filtered(pi, wi, xyz(slots[s]), xyz(slots0[s]), x0i, lrs, c2, acc, cnt);
+                }
             }
         }
     }
@@ -771,6 +784,7 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     __shared__ float4 sgl[kBlock];         // the particle's LRA rest distances, or the slot groups' boxes
     __shared__ float4 sx[kBlock];          // the particle's position (finalizing modes)
     __shared__ float4 sslot[kGridLraCached];
+    __shared__ float4 ssup[4 * (kLraGroupsMax / kLraSuper)];  // the slot super-groups' boxes
     __shared__ __align__(16) DomainParams sdom;
     static_assert(sizeof(DomainParams) % 16 == 0, "DomainParams is staged in 16-byte pieces");
     const GridTile tl = tiles[blockIdx.x];
@@ -814,7 +828,7 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     if (ns > kGridLraCached) {
         gsize = max(kLraGroupMin, (ns + kLraGroupsMax - 1) / kLraGroupsMax);
         ngroups = (ns + gsize - 1) / gsize;
-        lra_group_boxes(sgl, slots + s0, slots0 + s0, ns, gsize, ngroups, tid);
+        lra_group_boxes(sgl, ssup, slots + s0, slots0 + s0, ns, gsize, ngroups, tid);
     }
     grid_generator<kGHB, kGGA, kGGB>(a0 - 1 + gx, b0 - 1 + gy, R, sp, gx, gy, sst, sbd, gx, gy, sgr[tid],
                                      D.xpbd_bend);
@@ -829,8 +843,8 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     const float wi = pi4.w;
     vec3 acc = mk3(0, 0, 0);
     int cnt = 0;
-    grid_particle_sum<kGGA, kGGB>(a, b, R, i, hx, hy, sst, sbd, pi, wi, ns, s0, &sgl[tid], sslot, sgl, gsize,
-                                  ngroups, x0, slots, slots0, D.lrs, acc, cnt);
+    grid_particle_sum<kGGA, kGGB>(a, b, R, i, hx, hy, sst, sbd, pi, wi, ns, s0, &sgl[tid], sslot, sgl, ssup,
+                                  gsize, ngroups, x0, slots, slots0, D.lrs, acc, cnt);
     apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, &sx[tid], pout, x, v, status);
 }
 
