@@ -400,14 +400,28 @@ def run_reference(args) -> None:
 
 
 # ---------------------------------------------------------------------------- GPU arm
-def build_plain_solvers(wl, graphs=True):
+# --csr-kernels: grid cloths solved by the general CSR kernels (k_bend + k_solve) instead
+# of the implicit-topology tile kernel (same results; for profiling that path)
+CSR_KERNELS = False
+
+
+def new_solver(spec):
     import velvet_gb300 as vg
     from velvet_gb300 import workloads as W
 
+    s = vg.ClothSolver()
+    W.build_plain(spec, s)
+    if CSR_KERNELS:
+        vg._abi.check(vg.lib().vt_solver_use_grid_kernel(s.handle, 0), "vt_solver_use_grid_kernel")
+    return s
+
+
+def build_plain_solvers(wl, graphs=True):
+    import velvet_gb300 as vg
+
     solvers = []
     for spec in wl.cloths:
-        s = vg.ClothSolver()
-        W.build_plain(spec, s)
+        s = new_solver(spec)
         vg._abi.check(vg.lib().vt_solver_use_graphs(s.handle, 1 if graphs else 0), "vt_solver_use_graphs")
         solvers.append((s, spec, spec.particle_diameter()))
     return solvers
@@ -415,12 +429,10 @@ def build_plain_solvers(wl, graphs=True):
 
 def build_batch(wl):
     import velvet_gb300 as vg
-    from velvet_gb300 import workloads as W
 
     batch = vg.BatchSolver()
     for spec in wl.cloths:
-        s = vg.ClothSolver()
-        W.build_plain(spec, s)
+        s = new_solver(spec)
         batch.add(s)
         s.close()
     return batch
@@ -645,6 +657,8 @@ def main() -> None:
     ap.add_argument("--form", choices=["batched", "plain"], default="batched",
                     help="form run by --profile-frames")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--csr-kernels", action="store_true",
+                    help="solve grid cloths with the general CSR kernels instead of the tile kernel")
     ap.add_argument("--grid-tile", type=int, default=-1,
                     help="pin a grid kernel variant (velvet_gb300.GRID_VARIANTS index); -1 = autotune")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -665,6 +679,8 @@ def main() -> None:
     if args.impl == "reference":
         run_reference(args)
         return
+    global CSR_KERNELS
+    CSR_KERNELS = args.csr_kernels
     if args.grid_tile >= 0:
         import velvet_gb300 as vg
 
@@ -870,7 +886,9 @@ def main() -> None:
             "data": "synthetic grid cloths generated from the config (seeded), no dataset",
             "config": {"workload": wl.name, "form": "batched (one graph launch per frame for all cloths)",
                        "cloths_per_gpu": len(wl.cloths), "particles_per_gpu": n_tot,
-                       "substeps": wl.substeps, "iterations": wl.iterations, "grid_tile": grid_tile,
+                       "substeps": wl.substeps, "iterations": wl.iterations,
+                       "grid_tile": None if CSR_KERNELS else grid_tile,
+                       "kernels": "CSR (k_bend + k_solve)" if CSR_KERNELS else "grid tile (k_grid_iter)",
                        "l2": "inputs larger than L2 (working set ~%.1f GB)" % (n_tot * 500 / 1e9),
                        "parallelism": f"independent cloths per GPU x {world} GPU(s)"},
             "p50_frame_ms": statistics.median(per), "p99_frame_ms": pct(per, 0.99),
