@@ -535,6 +535,9 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
     int cnt = 0;
     // stretch: each entry is (other particle, rest length); this particle evaluates the
     // constraint as its first endpoint and takes -w_i * common
+    // unrolled by four: the entry and position loads of several constraints are in flight
+    // at once (the gathers are latency-bound; eight made it slower)
+#pragma unroll 4
     for (int e = st_off[i], e1 = st_off[i + 1]; e < e1; ++e) {
         const int2 en = st_ent[e];
         if (!VT_IN_RANGE(en.x, D.p_begin, D.p_begin + D.p_count, status)) continue;
@@ -560,6 +563,7 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
         }
     }
     // bending corners
+#pragma unroll 4
     for (int e = bd_off[i], e1 = bd_off[i + 1]; e < e1; ++e) {
         const float4 c = bcorr[bd_ent[e]];
         if (c.w != 0.0f) {
