@@ -203,30 +203,44 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
         const float diam = D.diameter;
         const bool far_ok = diam > 1e-18f && diam < 1e18f;
         const float far2 = (diam * diam) * kFarMargin;
-        // the next list entry is requested while this one is processed
-        uint32_t jn = __ldg(nb);
-        for (int k = 0; k < D.max_nbr; ++k) {
-            const uint32_t j = jn;
-            if (j == 0xffffffffu) break;
-            if (!VT_IN_RANGE(j, D.p_begin, D.p_begin + D.p_count, status)) break;
-            if (k + 1 < D.max_nbr) jn = __ldg(nb + (size_t)(k + 1) * stride);
-            const float4 pj4 = pin[j];
-            const float denom = wi + pj4.w;
-            if (denom <= 0) continue;
-            const vec3 pj = xyz(pj4);
-            const vec3 diff = pi - pj;
-            const float q = dot(diff, diff);
-            if (far_ok && q >= far2) continue;  // d >= diam without the square root
-            const float d = sqrtf(q);
-            if (d >= diam) continue;
-            const vec3 grad = diff / (d + VT_EPSILON);
-            const float lambda = (d - diam) / denom;
-            const vec3 common = grad * lambda;
-            count++;
-            delta = delta - common * wi;
-            const vec3 relvel = veli - (pj - xyz(x[j]));
-            const vec3 fr = friction_of(common, relvel, D.friction);
-            delta = delta + fr * wi;
+        // four list entries and their particles are requested together (loads beyond the
+        // list's end read a valid slot and are not used), then taken in list order
+        bool done = false;
+        for (int k0 = 0; k0 < D.max_nbr && !done; k0 += 4) {
+            uint32_t jq[4];
+            float4 pq[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                jq[u] = k0 + u < D.max_nbr ? __ldg(nb + (size_t)(k0 + u) * stride) : 0xffffffffu;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                pq[u] = pin[jq[u] - (uint32_t)D.p_begin < (uint32_t)D.p_count ? jq[u] : (uint32_t)D.p_begin];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (done) break;
+                const uint32_t j = jq[u];
+                if (j == 0xffffffffu || !VT_IN_RANGE(j, D.p_begin, D.p_begin + D.p_count, status)) {
+                    done = true;
+                    break;
+                }
+                const float4 pj4 = pq[u];
+                const float denom = wi + pj4.w;
+                if (denom <= 0) continue;
+                const vec3 pj = xyz(pj4);
+                const vec3 diff = pi - pj;
+                const float q = dot(diff, diff);
+                if (far_ok && q >= far2) continue;  // d >= diam without the square root
+                const float d = sqrtf(q);
+                if (d >= diam) continue;
+                const vec3 grad = diff / (d + VT_EPSILON);
+                const float lambda = (d - diam) / denom;
+                const vec3 common = grad * lambda;
+                count++;
+                delta = delta - common * wi;
+                const vec3 relvel = veli - (pj - xyz(x[j]));
+                const vec3 fr = friction_of(common, relvel, D.friction);
+                delta = delta + fr * wi;
+            }
         }
         if (count > 0) {
             const float c = (float)count;
