@@ -172,7 +172,7 @@ namespace {
 std::mutex g_tune_mu;
 int g_forced_variant = -1;
 int g_last_tuned = kGridDefaultVariant;
-std::vector<std::pair<std::vector<int64_t>, int>> g_tune_cache;  // signature -> shape
+std::vector<std::pair<std::vector<int64_t>, int>> g_tune_cache;  // signature -> variant
 }  // namespace
 
 int grid_variant_for(int tuned)
