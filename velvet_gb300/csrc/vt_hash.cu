@@ -160,8 +160,10 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
                int nbits, const uint32_t* __restrict__ hist, const uint32_t* __restrict__ digit_tot,
                int32_t ntiles, int32_t* __restrict__ status)
 {
-    __shared__ uint32_t off[256];
+    __shared__ uint32_t off[256];   // the tile's first output position per digit
+    __shared__ uint32_t lofs[256];  // the digit's first slot in the tile's sorted copy
     __shared__ uint32_t wcnt[kRsWarps][256];
+    __shared__ uint32_t sk[kRsTile], sv[kRsTile];  // the tile's pairs in output order
     const int ndig = 1 << nbits;
     const uint32_t mask = (uint32_t)ndig - 1;
     {
@@ -196,8 +198,8 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
         mr[j] = rank;
     }
     __syncthreads();
+    uint32_t run = 0;
     if ((int)threadIdx.x < ndig) {
-        uint32_t run = 0;
 #pragma unroll
         for (int w = 0; w < kRsWarps; ++w) {
             const uint32_t c = wcnt[w][threadIdx.x];
@@ -205,17 +207,34 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
             run += c;
         }
     }
+    {
+        uint32_t tot;
+        const uint32_t lex = block_exclusive_scan(run, &tot);
+        if ((int)threadIdx.x < ndig) lofs[threadIdx.x] = lex;
+    }
     __syncthreads();
+    // the tile's pairs into shared memory in (digit, stable rank) order, then written out
+    // by consecutive threads: each digit's run lands in consecutive output positions
 #pragma unroll
     for (int j = 0; j < kRsItems; ++j) {
         const int idx = wbase + j * 32 + lane;
         if (idx < n) {
             const uint32_t d = (mk[j] >> shift) & mask;
-            const uint32_t pos = off[d] + wcnt[warp][d] + mr[j];
-            if (!VT_IN_RANGE(pos, 0, n, status)) continue;
-            kout[pos] = mk[j];
-            vout[pos] = mv[j];
+            const uint32_t lp = lofs[d] + wcnt[warp][d] + mr[j];
+            if (!VT_IN_RANGE(lp, 0, kRsTile, status)) continue;
+            sk[lp] = mk[j];
+            sv[lp] = mv[j];
         }
+    }
+    __syncthreads();
+    const int count = min(kRsTile, n - (int)blockIdx.x * kRsTile);
+    for (int t = threadIdx.x; t < count; t += kBlock) {
+        const uint32_t key = sk[t];
+        const uint32_t d = (key >> shift) & mask;
+        const uint32_t pos = off[d] + ((uint32_t)t - lofs[d]);
+        if (!VT_IN_RANGE(pos, 0, n, status)) continue;
+        kout[pos] = key;
+        vout[pos] = sv[t];
     }
 }
 
