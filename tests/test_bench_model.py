@@ -34,3 +34,25 @@ def test_batched_workload_is_the_512_cloth_mix():
     assert wl.num_particles == 6_865_422
     assert bench.pits_per_frame(wl) == 6_865_422 * 5 * 10
     assert all(16 <= c.side <= 256 for c in wl.cloths)
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the CPU restatement on the host cores) prints one JSON
+    line with the metric, its own CPU baseline and an end-to-end figure without copies."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(bench.__file__).resolve().parent
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3"],
+                         cwd=root, capture_output=True, text=True, timeout=600, check=True).stdout
+    line = json.loads(out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["unit"] == "particle-iterations/s" and line["higher_is_better"] is True
+    assert line["metric"].startswith("particle-iterations/s")
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
+    assert cb["sample"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
