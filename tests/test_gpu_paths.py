@@ -173,6 +173,28 @@ def test_lra_slot_groups_skip_only_quiet_groups(side, rows, lrs):
     same(g.velocities(), o.velocities(), f"{rows * side} slots, stretchiness {lrs}, velocities")
 
 
+def test_moving_slots_keep_group_bounds_exact():
+    """A whole attached row (40 slots: groups of 16) dragged sideways and up frame by frame:
+    the slot groups' boxes are rebuilt from the current slot positions every iteration,
+    so skipping a group stays exact while the slots move."""
+    side = 40
+    spec = spec_of(side, 0.4, attached=list(range(side)))
+    o, g = Oracle(), vg.ClothSolver()
+    for s in (o, g):
+        W.build_plain(spec, s)
+    start = o.positions()[:side].copy()
+
+    def hook(f):
+        shift = np.array([0.03 * f, 0.01 * f, -0.02 * f], np.float32)
+        for s in (o, g):
+            for k in range(side):
+                s.set_attach_slot(k, start[k] + shift)
+
+    run_frames([o, g], spec, 6, frame_hook=hook)
+    same(g.positions(), o.positions(), "dragged row positions")
+    same(g.velocities(), o.velocities(), "dragged row velocities")
+
+
 def checkerboard_mesh(res, size):
     """A grid whose quad diagonals alternate direction: not the reference's mesh."""
     verts, _ = W.grid_mesh(res, size)
