@@ -872,8 +872,9 @@ def main() -> None:
         for s, _, _ in solvers:
             s.close()
 
+    # the CPU legs run once, at one GPU: at N > 1 the other ranks' GPUs would wait on them
     cpu, cpu_ref_solver, cpu_ref_solver_all = None, None, None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_single(args.workload, args.seed)
         cpu_ref_solver = cpu_reference_solver_single()
         cpu_ref_solver_all = cpu_reference_solver_all_cores(args.workload, args.seed)
