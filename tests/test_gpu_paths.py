@@ -246,7 +246,8 @@ def test_general_bending_adjacency_matches_the_oracle(mesh):
 
 
 @pytest.mark.parametrize("case", ["no_self_collision", "zero_iterations", "hash_every_substep",
-                                  "bend_compliance", "no_friction", "relaxation", "max_neighbors_8"])
+                                  "bend_compliance", "no_friction", "relaxation", "max_neighbors_8",
+                                  "max_speed_clamp", "no_damping", "heavy_damping", "hash_cells_larger"])
 def test_schedule_branches(case):
     p = vg.default_params()
     kw = {}
@@ -264,10 +265,20 @@ def test_schedule_branches(case):
         kw["relax"] = 1.4
     elif case == "max_neighbors_8":
         p.max_num_neighbors = 8
+    elif case == "no_damping":
+        p.damping = 0.0
+    elif case == "heavy_damping":
+        p.damping = 20.0
+    elif case == "hash_cells_larger":  # more candidates per bucket, more per-bucket truncation
+        p.hash_cell_size_scalar = 3.0
     spec = spec_of(18, 0.35)
     o, g = Oracle(p), vg.ClothSolver(p)
     for s in (o, g):
         W.build_plain(spec, s)
+        if case == "max_speed_clamp":  # AddCloth sets maxSpeed; lowered after it so Finalize clamps
+            q = s.params
+            q.max_speed = 0.4
+            s.params = q
     run_frames([o, g], spec, 6, **kw)
     same(g.positions(), o.positions(), case)
     same(g.velocities(), o.velocities(), case + " velocities")
