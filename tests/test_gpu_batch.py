@@ -46,6 +46,42 @@ def test_batch_equals_each_cloth_alone(graphs):
         assert np.array_equal(bits(batch.normals(k)), bits(o.normals())), f"cloth {k} normals"
 
 
+def test_batch_mixing_kernel_kinds_equals_each_cloth_alone():
+    """One batch holding grid cloths on the tile kernel, grid cloths on the CSR kernels
+    (vt_solver_use_grid_kernel off) and a cloth whose 24 LRA slots take the slot-group
+    path at a nonzero slot offset: every kind of domain in one frame, each cloth's bits
+    those it has alone."""
+    wl = mixed(6, seed=11)
+    specs = list(wl.cloths)
+    side = 24
+    specs.append(W.ClothSpec(side, 0.02, W.horizontal_cloth(side, 0.02, 0.5),
+                             list(range(0, side)), specs[0].colliders))
+    csr = {1, 4}
+    batch = vg.BatchSolver()
+    alone = []
+    for k, spec in enumerate(specs):
+        pair = []
+        for _ in range(2):
+            s = vg.ClothSolver()
+            W.build_plain(spec, s)
+            if k in csr:
+                assert vg.lib().vt_solver_use_grid_kernel(s.handle, 0) == 0
+            pair.append(s)
+        batch.add(pair[0])
+        alone.append((pair[1], spec))
+    for f in range(6):
+        batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin)
+        for o, spec in alone:
+            o.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin, spec.particle_diameter())
+    batch.sync()
+    for k, (o, spec) in enumerate(alone):
+        o.sync()
+        assert np.array_equal(bits(batch.positions(k)), bits(o.positions())), f"cloth {k} positions"
+        assert np.array_equal(bits(batch.velocities(k)), bits(o.velocities())), f"cloth {k} velocities"
+
+
 def test_batch_matches_oracle_with_moving_collider():
     wl = mixed(3, seed=5)
     batch = vg.BatchSolver()
