@@ -316,24 +316,28 @@ vt_status World::autotune(cudaStream_t st, bool may_time)
         cudaEvent_t e0, e1;
         VT_CUDA(cudaEventCreate(&e0), "event");
         VT_CUDA(cudaEventCreate(&e1), "event");
-        float best_ms = 0;
-        for (int v = 0; v < kGridVariants; ++v) {
-            vt_status r = set_grid_variant(v);
-            if (r != VT_OK) return r;
-            Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles, n_gptiles, grid_variant};
-            VT_CUDA(launch_grid_iter(L, 0, 1, SOLVE_PLAIN), "tune warm-up");
-            VT_CUDA(cudaEventRecord(e0, st), "event");
-            for (int k = 0; k < 3; ++k) VT_CUDA(launch_grid_iter(L, 0, 1, SOLVE_PLAIN), "tune");
-            VT_CUDA(cudaEventRecord(e1, st), "event");
-            VT_CUDA(cudaEventSynchronize(e1), "tune sync");
-            float ms = 0;
-            VT_CUDA(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
-            launches += 4;
-            if (best < 0 || ms < best_ms) {
-                best = v;
-                best_ms = ms;
+        // three interleaved rounds over the variants (a warm-up and three timed launches
+        // each), the lowest total kept: variants within a percent of each other are ranked
+        // under the same drift of clocks and caches
+        constexpr int kRounds = 3;
+        float total[kGridVariants] = {};
+        for (int round = 0; round < kRounds; ++round)
+            for (int v = 0; v < kGridVariants; ++v) {
+                vt_status r = set_grid_variant(v);
+                if (r != VT_OK) return r;
+                Launch L{&d, n_ptiles, n_btiles, n_particles, st, n_stiles, n_gtiles, n_gptiles, grid_variant};
+                VT_CUDA(launch_grid_iter(L, 0, 1, SOLVE_PLAIN), "tune warm-up");
+                VT_CUDA(cudaEventRecord(e0, st), "event");
+                for (int k = 0; k < 3; ++k) VT_CUDA(launch_grid_iter(L, 0, 1, SOLVE_PLAIN), "tune");
+                VT_CUDA(cudaEventRecord(e1, st), "event");
+                VT_CUDA(cudaEventSynchronize(e1), "tune sync");
+                float ms = 0;
+                VT_CUDA(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+                launches += 4;
+                total[v] += ms;
             }
-        }
+        for (int v = 0; v < kGridVariants; ++v)
+            if (best < 0 || total[v] < total[best]) best = v;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         std::lock_guard<std::mutex> lock(g_tune_mu);
