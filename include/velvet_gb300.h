@@ -358,6 +358,7 @@ typedef struct vt_server_config {
 #define VT_REQ_ACTIVE 1
 #define VT_REQ_DONE   2
 #define VT_REQ_FAILED 3  /* its state became NaN / Inf: evicted, no result (VT_ERR_NUMERIC) */
+#define VT_REQ_CANCELLED 4  /* cancelled by the client: dropped or evicted, no result */
 
 typedef struct vt_server_tick_info {
     int32_t  admitted, retired, active, queued;
@@ -373,6 +374,7 @@ typedef struct vt_server_stats {
     double   p50_frame_ms, p99_frame_ms;  /* over all (request, frame) pairs                 */
     uint64_t bytes_in_use, bytes_budget;
     uint64_t requests_failed;      /* evicted after a NaN / Inf fault, the others unaffected */
+    uint64_t requests_cancelled;   /* vt_server_cancel of a queued or active request         */
 } vt_server_stats;
 
 vt_status vt_server_create(const vt_server_config* cfg, vt_server** out);
@@ -416,6 +418,13 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info);
  * its slot's fault flag; the tick that sees the flag evicts it at the next tick
  * (VT_REQ_FAILED, counted in requests_failed) and no other request is affected. */
 vt_status vt_server_poll(vt_server* s, int64_t request_id, int32_t* state, int32_t* frames_done);
+
+/* Cancels a request (a client that went away): a queued one leaves the queue at once; an
+ * active one is evicted at the next tick, its range and slot returned as for a fault,
+ * the requests beside it unaffected.  Either way it ends as VT_REQ_CANCELLED with no
+ * result.  VT_ERR_STATE once its last frame is enqueued (it finishes normally) or it has
+ * ended. */
+vt_status vt_server_cancel(vt_server* s, int64_t request_id);
 
 /* Final positions of a finished request (count = its particle count) into host memory;
  * VT_ERR_NUMERIC for an evicted request. */

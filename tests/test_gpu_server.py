@@ -189,6 +189,41 @@ def test_a_request_that_turns_nan_is_evicted_and_the_others_are_untouched():
     assert stats.requests_failed == 1 and stats.requests_done == 2
 
 
+def test_cancelled_requests_leave_and_the_others_are_untouched():
+    """A client that goes away: one request cancelled while queued (it never runs), one
+    while active (evicted at the next tick, its range and slot reused by the queue); both
+    end as VT_REQ_CANCELLED without a result, and the other requests keep their bits."""
+    srv = vg.ClothServer(hbm_budget_bytes=1 << 30, max_cloths=2, substeps=3, iterations=4)
+    plan = [(request(20, 0.5), 6), (request(24, 0.55), 9), (request(16, 0.6), 5), (request(18, 0.5), 4)]
+    ids = []
+    for spec, frames in plan:
+        s = registered(spec)
+        ids.append(srv.submit(s, frames))
+        s.close()
+    srv.tick()                 # two slots: requests 0 and 1 active, 2 and 3 queued
+    srv.cancel(ids[2])         # queued: leaves at once
+    assert srv.poll(ids[2])[0] == _abi.REQ_CANCELLED
+    srv.tick()
+    srv.cancel(ids[1])         # active: evicted by the next tick, request 3 takes its slot
+    for _ in range(60):
+        info = srv.tick()
+        if info.active == 0 and info.queued == 0:
+            break
+    for k in (1, 2):
+        assert srv.poll(ids[k])[0] == _abi.REQ_CANCELLED
+        with pytest.raises(vg.VtError) as e:
+            srv.result(ids[k])
+        assert e.value.status == _abi.VT_ERR_STATE
+        with pytest.raises(vg.VtError):
+            srv.cancel(ids[k])  # already ended
+    for k in (0, 3):
+        spec, frames = plan[k]
+        assert srv.poll(ids[k]) == (_abi.REQ_DONE, frames)
+        assert np.array_equal(bits(srv.result(ids[k])), bits(alone(spec, frames)))
+    stats = srv.stats()
+    assert stats.requests_cancelled == 2 and stats.requests_done == 2 and stats.requests_failed == 0
+
+
 def test_rejects_non_grid_and_oversize():
     srv = vg.ClothServer(hbm_budget_bytes=1 << 27, max_cloths=2)  # ~300k particles of arena
     s = vg.ClothSolver()

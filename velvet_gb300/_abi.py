@@ -105,6 +105,7 @@ class VtServerStats(C.Structure):
         ("particle_iterations", C.c_double), ("gpu_ms", C.c_double),
         ("p50_frame_ms", C.c_double), ("p99_frame_ms", C.c_double),
         ("bytes_in_use", C.c_uint64), ("bytes_budget", C.c_uint64), ("requests_failed", C.c_uint64),
+        ("requests_cancelled", C.c_uint64),
     ]
 
 
@@ -133,7 +134,7 @@ class VtRenderParams(C.Structure):
     ]
 
 
-REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, 4
 
 
 class VtHashParams(C.Structure):
@@ -212,6 +213,7 @@ SIGNATURES: dict[str, tuple] = {
                                     C.POINTER(C.c_int64)]),
     "vt_server_tick": (I32, [P, P, C.POINTER(VtServerTickInfo)]),
     "vt_server_poll": (I32, [P, C.c_int64, PI32, PI32]),
+    "vt_server_cancel": (I32, [P, C.c_int64]),
     "vt_server_result": (I32, [P, C.c_int64, P, U32]),
     "vt_server_stats_get": (I32, [P, C.POINTER(VtServerStats)]),
     "vt_tuning_set_grid_tile": (I32, [I32]),

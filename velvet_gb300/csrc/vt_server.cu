@@ -53,6 +53,7 @@ struct Request {
     const float* res_pin = nullptr;  // result in a pinned ring (copied out when complete)
     std::vector<float> result;
     bool failed = false;  // a frame produced NaN / Inf state: evicted, reported, no result
+    bool cancelled = false;  // vt_server_cancel while active: evicted at the next tick
     // described grid cloth (vt_server_submit_grid): built on the device at admission,
     // h holds its parameters, slots and colliders but no particle arrays
     bool described = false;
@@ -602,10 +603,10 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
     // that frame on the stream, so their range and slot are free for this tick's admissions
     for (int32_t sid = 0; sid < (int32_t)s->slot.size(); ++sid) {
         Request* r = s->slot[sid];
-        if (!r || (r->enq < r->frames && !r->failed)) continue;
+        if (!r || (r->enq < r->frames && !r->failed && !r->cancelled)) continue;
         // the slot's fault flag is cleared before a new request can take the slot
         VT_TRY_CUDA(cudaMemsetAsync(s->d.status + 1 + sid, 0, 4, st), "clear fault flag");
-        if (r->failed) {  // evicted: no result, the range and slot return at once
+        if (r->failed || r->cancelled) {  // evicted: no result, the range and slot return at once
             k_fill_i32<<<(unsigned)((r->n + 255) / 256), 256, 0, st>>>(s->pdom + r->pb, (int64_t)r->n, -1);
             VT_TRY_CUDA(cudaGetLastError(), "clear domain ids");
             s->launches += 1;
@@ -614,9 +615,12 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
             s->n_active -= 1;
             s->slot[sid] = nullptr;
             r->sid = -1;
-            r->state = VT_REQ_FAILED;
+            r->state = r->failed ? VT_REQ_FAILED : VT_REQ_CANCELLED;
             r->h = vt::HostSolver{};
-            s->stats.requests_failed += 1;
+            if (r->failed)
+                s->stats.requests_failed += 1;
+            else
+                s->stats.requests_cancelled += 1;
             s->tables_dirty = true;
             ti.retired += 1;
             continue;
@@ -757,6 +761,29 @@ vt_status vt_server_poll(vt_server* s, int64_t id, int32_t* state, int32_t* fram
     return VT_OK;
 }
 
+vt_status vt_server_cancel(vt_server* s, int64_t id)
+{
+    VT_CHECK(s, VT_ERR_INVALID_ARGUMENT, "NULL server");
+    auto it = s->reqs.find(id);
+    VT_CHECK(it != s->reqs.end(), VT_ERR_NOT_FOUND, "unknown request");
+    Request* r = it->second.get();
+    if (r->state == VT_REQ_QUEUED) {
+        for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+            if (*q == r) {
+                s->queue.erase(q);
+                break;
+            }
+        r->state = VT_REQ_CANCELLED;
+        r->h = vt::HostSolver{};
+        s->stats.requests_cancelled += 1;
+        return VT_OK;
+    }
+    VT_CHECK(r->state == VT_REQ_ACTIVE && r->sid >= 0 && r->enq < r->frames && !r->failed, VT_ERR_STATE,
+             "the request has its last frame enqueued or has ended");
+    r->cancelled = true;  // evicted by the next tick's retire step
+    return VT_OK;
+}
+
 vt_status vt_server_result(vt_server* s, int64_t id, float* dst, uint32_t count)
 {
     VT_CHECK(s && dst, VT_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -764,6 +791,7 @@ vt_status vt_server_result(vt_server* s, int64_t id, float* dst, uint32_t count)
     VT_CHECK(it != s->reqs.end(), VT_ERR_NOT_FOUND, "unknown request");
     const Request& r = *it->second;
     VT_CHECK(r.state != VT_REQ_FAILED, VT_ERR_NUMERIC, "the request's state became NaN / Inf; it was evicted");
+    VT_CHECK(r.state != VT_REQ_CANCELLED, VT_ERR_STATE, "the request was cancelled");
     VT_CHECK(r.state == VT_REQ_DONE, VT_ERR_STATE, "request not finished");
     VT_CHECK(count == r.n, VT_ERR_INVALID_ARGUMENT, "count must equal the request's particle count");
     std::memcpy(dst, r.result.data(), 12 * (size_t)count);

@@ -449,6 +449,10 @@ class ClothServer:
         check(lib().vt_server_poll(self._h, rid, C.byref(st), C.byref(done)), "vt_server_poll")
         return st.value, done.value
 
+    def cancel(self, rid: int) -> None:
+        """vt_server_cancel: a queued request leaves at once, an active one at the next tick."""
+        check(lib().vt_server_cancel(self._h, rid), "vt_server_cancel")
+
     def result(self, rid: int) -> np.ndarray:
         n = self.sizes[rid]
         out = np.empty((n, 3), np.float32)
