@@ -500,7 +500,8 @@ vt_status vt_profiler_read(vt_stage_time* out, uint32_t capacity, uint32_t* coun
  * empty cells) and cell_end[table_size] for occupied cells, and writes the column-major
  * neighbour lists with the initial-position filter.  Sort scratch space is allocated
  * on first use per device and kept until the library is unloaded (the reference keeps
- * a static cub buffer).  Enqueued on `stream`. */
+ * a static cub buffer), so cudaDeviceReset after the first call on a device is not
+ * supported.  Enqueued on `stream`. */
 vt_status vt_hash_objects(uint32_t* particle_hash, uint32_t* particle_index,
                           uint32_t* cell_start, uint32_t* cell_end, uint32_t* neighbors,
                           const float* positions, const float* original_positions,
@@ -521,7 +522,9 @@ vt_status vt_hash_objects(uint32_t* particle_hash, uint32_t* particle_index,
  *     streams, or different host threads) race and corrupt each other's results;
  *     serialise them on one stream.
  *   - Nothing in the scratch needs to start at zero, so a previous call's contents do
- *     not affect the result. */
+ *     not affect the result.
+ *   - The array's device address is kept for the life of the process: calling
+ *     cudaDeviceReset on a device after its first call is not supported. */
 #define VT_HASH_NOALLOC_MAX_OBJECTS 262144
 vt_status vt_hash_objects_noalloc(uint32_t* particle_hash, uint32_t* particle_index,
                                   uint32_t* cell_start, uint32_t* cell_end, uint32_t* neighbors,

@@ -13,8 +13,11 @@
 // objects' worth of scratch (about 2.2 MB).  Every GPU on which the library is loaded
 // holds it until the process exits.  In host code its name is only a host-side stand-in
 // for the device variable, never a device address: the address is obtained once per
-// device with cudaGetSymbolAddress and passed to the kernels.
+// device with cudaGetSymbolAddress and passed to the kernels.  The address is kept for
+// the life of the process, so a cudaDeviceReset after the first call on a device is not
+// supported (the module would be reloaded and the kept address would be stale).
 #include <mutex>
+#include <new>
 
 #include "vt_host.h"
 
@@ -54,11 +57,9 @@ vt_status scratch_for_current_device(uint32_t** out)
 
 }  // namespace
 
-extern "C" vt_status vt_hash_objects_noalloc(uint32_t* particle_hash, uint32_t* particle_index,
-                                             uint32_t* cell_start, uint32_t* cell_end,
-                                             uint32_t* neighbors, const float* positions,
-                                             const float* original_positions,
-                                             const vt_hash_params* hp, void* stream)
+static vt_status hash_objects_noalloc(uint32_t* particle_hash, uint32_t* particle_index, uint32_t* cell_start,
+                                      uint32_t* cell_end, uint32_t* neighbors, const float* positions,
+                                      const float* original_positions, const vt_hash_params* hp, void* stream)
 {
     if (!hp || !cell_start) {
         vt::set_error("params and cell_start must not be NULL");
@@ -87,6 +88,11 @@ extern "C" vt_status vt_hash_objects_noalloc(uint32_t* particle_hash, uint32_t* 
     uint32_t* vals_tmp = keys_tmp + cap;
     uint32_t* hist = vals_tmp + cap;
     uint32_t* digit_tot = hist + vt::radix_hist_words(n);
+    // the sort's layout must fit the fixed array (its tile size lives in vt_hash.cu)
+    if (2 * cap + vt::radix_hist_words(n) + 256 > kScratchWords) {
+        vt::set_error("vt_hash_objects_noalloc: the sort scratch for this table exceeds the fixed array");
+        return VT_ERR_CAPACITY;
+    }
     // Nothing in the scratch has to start at zero: the sort writes every histogram, total
     // and temporary key before reading it, so the previous call's contents are harmless.
     cudaError_t e = vt::hash_objects_f3(particle_hash, particle_index, cell_start, cell_end, neighbors,
@@ -94,4 +100,22 @@ extern "C" vt_status vt_hash_objects_noalloc(uint32_t* particle_hash, uint32_t* 
                                         digit_tot, (cudaStream_t)stream);
     if (e != cudaSuccess) return vt::cuda_fail(e, "hash_objects (no-alloc)");
     return VT_OK;
+}
+
+extern "C" vt_status vt_hash_objects_noalloc(uint32_t* particle_hash, uint32_t* particle_index,
+                                             uint32_t* cell_start, uint32_t* cell_end,
+                                             uint32_t* neighbors, const float* positions,
+                                             const float* original_positions,
+                                             const vt_hash_params* hp, void* stream)
+{
+    try {  // no C++ exception (e.g. from the mutex) crosses the C ABI
+        return hash_objects_noalloc(particle_hash, particle_index, cell_start, cell_end, neighbors, positions,
+                                    original_positions, hp, stream);
+    } catch (const std::bad_alloc&) {
+        vt::set_error("host allocation failed");
+        return VT_ERR_OUT_OF_MEMORY;
+    } catch (...) {
+        vt::set_error("unexpected host exception");
+        return VT_ERR_STATE;
+    }
 }

@@ -778,7 +778,9 @@ vt_status vt_server_cancel(vt_server* s, int64_t id)
         s->stats.requests_cancelled += 1;
         return VT_OK;
     }
-    VT_CHECK(r->state == VT_REQ_ACTIVE && r->sid >= 0 && r->enq < r->frames && !r->failed, VT_ERR_STATE,
+    VT_CHECK(!(r->state == VT_REQ_ACTIVE && r->failed), VT_ERR_STATE,
+             "the request's state became NaN / Inf; it ends as failed and is evicted at the next tick");
+    VT_CHECK(r->state == VT_REQ_ACTIVE && r->sid >= 0 && r->enq < r->frames, VT_ERR_STATE,
              "the request has its last frame enqueued or has ended");
     r->cancelled = true;  // evicted by the next tick's retire step
     return VT_OK;
