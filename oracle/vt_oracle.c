@@ -28,12 +28,16 @@
  * vo_acosf below — the Maclaurin series of arcsin with the half-angle identity — so the
  * two sides agree bit for bit; its distance from the exact arccos is checked in tests.
  *
- * Parity status: UNPINNED against the reference itself.  The reference ships no tests,
- * golden vectors or fixtures for this path, and its sources cannot be built here
- * (they need glm, fmt, imgui, glad/GLFW, none of which exist on either machine), so no
- * reference output exists to compare against.  This restatement is pinned instead by
- * known-answer tests computed independently in tests/ (hash keys, single-constraint
- * analytic cases, SDF projections, acos error bound).
+ * Parity status: PINNED to the reference's own kernel code.  oracle/refemu compiles the
+ * reference's Velvet/VtClothSolverGPU.cu and Velvet/SpatialHashGPU.cu unmodified for the
+ * CPU (make -C oracle ref -> oracle/_ref/libvr_ref.so, atomics in thread order, acos from
+ * vo_acosf below), and this restatement reproduces its outputs bit for bit: the committed
+ * fixtures tests/golden/ref_*.npz (every collider kind, the schedule's branches, a row of
+ * attachments, two colliding cloths, HashObjects on a cloud) and, where the reference tree
+ * is present, the small configuration's 64x64 cloth live (tests/test_ref_pinning.py).  What
+ * stays unpinned: glm's own evaluation order (the stand-in glm assumes the orders above)
+ * and CUDA's acosf.  Known-answer tests in tests/ check hash keys, single-constraint
+ * analytic cases, SDF projections and the acos error bound independently.
  */
 #include <math.h>
 #include <stdint.h>
