@@ -1,8 +1,10 @@
-"""GPU checks at the configurations' full sizes, where the oracle is too slow to follow
-every frame: the large cloth against the oracle for a few frames, and size-independent
-properties for the stress cloth and the 512-cloth mix — two different kernels agree bit
-for bit (the implicit-topology tile kernel and the general CSR kernels), a batch equals
-each cloth simulated alone, and reruns are identical."""
+"""GPU checks at the configurations' full sizes and shapes: the large cloth against the
+oracle for 6 frames (and 60 in a slow test), a stress-shaped cloth (seeded drop height
+and spheres, the whole top row attached, 8 x 10) against the oracle for 20 frames at
+128x128, and size-independent properties where the oracle is too slow to follow: for the
+1024x1024 stress cloth two different kernels agree bit for bit (the implicit-topology
+tile kernel and the general CSR kernels) and reruns are identical; the 512-cloth mix as
+one batch equals each cloth simulated alone."""
 
 import numpy as np
 import pytest
@@ -43,6 +45,49 @@ def test_large_config_moving_sphere_matches_the_oracle():
     same(g.positions(), o.positions(), "large positions")
     same(g.velocities(), o.velocities(), "large velocities")
     same(g.normals(), o.normals(), "large normals")
+
+
+@pytest.mark.slow
+def test_large_config_matches_the_oracle_for_60_frames():
+    """256x256 cloth, moving sphere, 5 x 20: bit-exact at frames 20, 40 and 60."""
+    wl = W.large()
+    spec = wl.cloths[0]
+    g, o = vg.ClothSolver(), Oracle()
+    for s in (g, o):
+        W.build_plain(spec, s)
+    for f in range(60):
+        frame(wl, (g, o), spec, f)
+        if (f + 1) % 20 == 0:
+            g.sync()
+            same(g.positions(), o.positions(), f"large positions after {f + 1} frames")
+            same(g.velocities(), o.velocities(), f"large velocities after {f + 1} frames")
+    same(g.normals(), o.normals(), "large normals after 60 frames")
+
+
+@pytest.mark.parametrize("grid", [True, False], ids=["tile", "csr"])
+def test_stress_shaped_cloth_matches_the_oracle(grid):
+    """The stress configuration's shape at 128x128: drop height U(0.5, 1.5) m and four
+    spheres of radius U(0.1, 0.4) m from seed 0, plane, the whole top row attached (128
+    LRA slots: eight slot groups of 16 in two super-groups, the tile kernel's group
+    skips), 8 substeps x 10 iterations, bit-exact against the oracle at frames 1, 5, 10,
+    15 and 20, through the tile kernel and through the CSR kernels."""
+    wl = W.stress(frames=20, seed=0, side=128)
+    spec = wl.cloths[0]
+    g, o = vg.ClothSolver(), Oracle()
+    for s in (g, o):
+        W.build_plain(spec, s)
+    assert vg.lib().vt_solver_use_grid_kernel(g.handle, 1 if grid else 0) == 0
+    moved = 0.0
+    x0 = o.positions()
+    for f in range(wl.frames):
+        frame(wl, (g, o), spec, f)
+        if f + 1 in (1, 5, 10, 15, 20):
+            g.sync()
+            same(g.positions(), o.positions(), f"stress-shaped positions after {f + 1} frames")
+            same(g.velocities(), o.velocities(), f"stress-shaped velocities after {f + 1} frames")
+            moved = float(np.abs(o.positions() - x0).max())
+    same(g.normals(), o.normals(), "stress-shaped normals after 20 frames")
+    assert moved > 0.1, "the cloth should have fallen"
 
 
 def test_stress_config_tile_and_csr_kernels_agree_and_rerun_identically():
