@@ -19,9 +19,13 @@ Arms:
                          The JSON line also carries the plain (one cloth at a time)
                          drop-in solver's rate and p50/p99 frame latency, the dominant
                          kernel's roofline, and the CPU oracle timed on a bounded sample.
-  --impl reference       the CPU restatement of the reference solver (the oracle; the
-                         reference's own sources cannot be built on these machines),
-                         all host cores, one process per core, bounded sample.
+  --impl reference       the CPU restatement of the reference solver (the oracle, which
+                         reproduces the reference's own kernels bit for bit; those kernels
+                         compile for the CPU only where the reference tree is, not on the
+                         GPU machine), all host cores, one process per core, bounded sample.
+  --variant fast|exact   the library build the ours arm times (default fast: contracted
+                         arithmetic within the stated tolerance of the oracle; the JSON
+                         line also carries the exact build's rate, `exact_build`).
 Multi-GPU (torchrun): each rank runs its own copy of the workload (cloths are
 independent; no collective on the data path) -> weak scaling.
 """
@@ -389,7 +393,8 @@ def run_reference(args) -> None:
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * statistics.mean(step_times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic grid cloths (seeded), CPU restatement of the reference GPU solver",
+        "data": "synthetic grid cloths (seeded), CPU restatement of the reference GPU solver "
+                "(bit-identical to the reference's own kernels run on the CPU)",
         "config": {"workload": wl.name, "cloths_sampled": len(idx), "substeps": wl.substeps,
                    "iterations": wl.iterations},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(chunks), "kind": "port",
@@ -514,21 +519,26 @@ def pct(v, q):
     return s[min(len(s) - 1, int(q * len(s)))]
 
 
-def run_serving(args) -> None:
-    """Served form: Poisson arrivals (--rate req/s for --duration s), each request one
+def serving_legs(args, duration: float, plain_seconds: float) -> tuple[dict, dict]:
+    """Served form: Poisson arrivals (args.rate req/s for `duration` s), each request one
     grid cloth with side log-uniform in [16, 512] and a frame count uniform in [30, 300],
     admitted by the HBM budget (--budget-gb) and an active-particle cap, one frame for all
     active requests per tick.  Requests wait in a front-end backlog and enter the
-    server's queue as it drains.  Reports aggregate particle-iterations/s over the wall
-    time, p50/p99 frame latency, and the plain solver run one request at a time on the
-    same arrival stream for a bounded time."""
+    server's queue as it drains.  Returns the served leg (aggregate particle-iterations/s
+    over the wall time, p50/p99 frame latency, request latency from arrival to admission
+    and to completion) and the plain solver run one request at a time on the same
+    arrival stream for `plain_seconds`.  Both legs are timed alike: registration of a
+    request's cloth on the host is outside both timed regions (the served leg's payloads
+    are built before its loop; the plain leg's registration time is measured and taken
+    out), and neither leg synchronises per frame (the plain leg records an event pair per
+    frame and reads them once per request)."""
     import torch
 
     import velvet_gb300 as vg
     from velvet_gb300 import workloads as W
 
     rng = np.random.default_rng(args.seed)
-    n_req = int(args.rate * args.duration * 1.5) + 16
+    n_req = int(args.rate * duration * 1.5) + 16
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
     sides = np.rint(np.exp(rng.uniform(math.log(16), math.log(512), n_req))).astype(int)
     frames = rng.integers(30, 301, n_req)
@@ -564,10 +574,9 @@ def run_serving(args) -> None:
     # work): build the payload of every size that can arrive before the timed loop
     tb = time.perf_counter()
     if not args.described:
-        for side in sorted(set(int(v) for v in sides)):
+        for side in sorted(set(int(v) for v in sides[: int(args.rate * duration * 1.2) + 16])):
             template(side)
     build_s = time.perf_counter() - tb
-    torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     srv = vg.ClothServer(int(args.budget_gb * (1 << 30)), max_cloths=4096,
                          max_active_particles=args.max_active_particles, substeps=S, iterations=It)
@@ -579,10 +588,12 @@ def run_serving(args) -> None:
     k = 0
     backlog: list[int] = []
     ticks, admitted, active_samples = 0, 0, []
+    outstanding: dict[int, int] = {}  # request id -> arrival index
+    t_admit, t_done = {}, {}
     t0 = time.perf_counter()
     while True:
         now = time.perf_counter() - t0
-        if now >= args.duration:
+        if now >= duration:
             break
         while k < n_req and arrivals[k] <= now:
             backlog.append(k)
@@ -590,58 +601,92 @@ def run_serving(args) -> None:
         info_q = 0
         while backlog and info_q < 2:
             j = backlog.pop(0)
-            submit(srv, int(sides[j]), int(frames[j]))
+            outstanding[submit(srv, int(sides[j]), int(frames[j]))] = j
             info_q += 1
         info = srv.tick(stream)
         ticks += 1
         admitted += info.admitted
         active_samples.append(info.active_particles)
+        now = time.perf_counter() - t0
+        for rid in list(outstanding):
+            state, _ = srv.poll(rid)
+            j = outstanding[rid]
+            if state != 0 and j not in t_admit:  # left the queue
+                t_admit[j] = now
+            if state >= 2:  # done, failed or cancelled
+                t_done[j] = now
+                del outstanding[rid]
     wall = time.perf_counter() - t0
     st = srv.stats()
     pits = st.particle_iterations - base.particle_iterations
+    wait = [t_admit[j] - arrivals[j] for j in t_admit]
+    resp = [t_done[j] - arrivals[j] for j in t_done]
     served = {"value": pits / wall, "unit": UNIT, "wall_s": wall, "ticks": ticks,
               "p50_frame_ms": st.p50_frame_ms, "p99_frame_ms": st.p99_frame_ms,
+              "frame_latency": "event-timed GPU time of the tick's frame, weighted by its requests",
               "arrived": k, "admitted": admitted, "completed": int(st.requests_done - base.requests_done),
               "backlog_at_end": len(backlog),
+              "request_wait_s": {"p50": statistics.median(wait) if wait else None,
+                                 "p99": pct(wait, 0.99) if wait else None,
+                                 "what": "arrival to admission (queueing; the stream asks for more than one "
+                                         "GPU sustains, so the backlog grows through the run)"},
+              "request_latency_s": {"p50": statistics.median(resp) if resp else None,
+                                    "p99": pct(resp, 0.99) if resp else None, "what": "arrival to last frame"},
               "mean_active_particles": float(np.mean(active_samples)) if active_samples else 0.0,
               "gpu_busy_frac": (st.gpu_ms - base.gpu_ms) / 1000.0 / wall,
               "payload_build_s_untimed": build_s, "distinct_sizes": len(templates) or len(described),
               "submission": "described grid cloths, built on the device at admission" if args.described
               else "registered solvers (host-built constraint arrays)"}
     srv.close()
+    for s, _ in templates.values():
+        s.close()
 
-    # the plain solver, one request at a time, same stream of requests, bounded time
-    p_pits, p_frames, p_ms = 0, [], 0.0
+    # the plain solver, one request at a time, same stream of requests, bounded time;
+    # host registration of each request is measured and taken out of the wall time
+    p_pits, p_frames, reg_s = 0, [], 0.0
+    pool = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(301)]
+    torch.cuda.synchronize()
     t1 = time.perf_counter()
     j = 0
-    while time.perf_counter() - t1 < args.plain_seconds and j < n_req:
+    while time.perf_counter() - t1 - reg_s < plain_seconds and j < n_req:
+        tr = time.perf_counter()
         spec = spec_of(int(sides[j]))
         s = vg.ClothSolver()
         W.build_plain(spec, s)
         d = spec.particle_diameter()
-        for f in range(int(frames[j])):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
+        reg_s += time.perf_counter() - tr
+        nf = int(frames[j])
+        for f in range(nf):
+            pool[f][0].record(stream)
             s.simulate(float(W.FRAME_DT), S, It, 1.0, 0.1, 0.06, d, stream)
-            e1.record(stream)
-            e1.synchronize()
-            p_frames.append(e0.elapsed_time(e1))
+            pool[f][1].record(stream)
             p_pits += spec.num_particles * S * It
-            if time.perf_counter() - t1 >= args.plain_seconds:
-                break
+        pool[nf - 1][1].synchronize()
+        p_frames.extend(pool[f][0].elapsed_time(pool[f][1]) for f in range(nf))
         s.close()
         j += 1
-    p_wall = time.perf_counter() - t1
+    p_wall = time.perf_counter() - t1 - reg_s
     plain = {"value": p_pits / p_wall, "unit": UNIT, "wall_s": p_wall, "requests": j,
+             "registration_s_excluded": reg_s,
              "p50_frame_ms": statistics.median(p_frames), "p99_frame_ms": pct(p_frames, 0.99)}
-    line = {"metric": METRIC, "value": served["value"], "unit": UNIT, "n_gpus": 1, "steps": ticks,
-            "warmup": 1, "ms_per_step": 1000 * wall / max(1, ticks), "higher_is_better": True,
+    return served, plain
+
+
+def run_serving(args) -> None:
+    """--workload serving: the served and plain legs for --duration / --plain-seconds."""
+    import torch
+
+    torch.cuda.set_device(0)
+    served, plain = serving_legs(args, args.duration, args.plain_seconds)
+    S, It = 5, 10
+    line = {"metric": METRIC, "value": served["value"], "unit": UNIT, "n_gpus": 1, "steps": served["ticks"],
+            "warmup": 1, "ms_per_step": 1000 * served["wall_s"] / max(1, served["ticks"]), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": f"synthetic Poisson request stream, seed {args.seed}",
             "config": {"workload": "serving", "rate_per_s": args.rate, "duration_s": args.duration,
                        "side": "log-uniform [16, 512]", "frames": "uniform [30, 300]",
                        "budget_gb": args.budget_gb, "max_active_particles": args.max_active_particles,
-                       "substeps": S, "iterations": It},
+                       "substeps": S, "iterations": It, "library": os.environ.get("VT_VARIANT", "exact")},
             "served": served, "plain": plain, "served_over_plain": served["value"] / plain["value"],
             "p50_frame_ms": served["p50_frame_ms"], "p99_frame_ms": served["p99_frame_ms"]}
     print(json.dumps(line), flush=True)
@@ -670,12 +715,26 @@ def main() -> None:
     ap.add_argument("--described", action="store_true",
                     help="serving: submit grid cloths by description (built on the device)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device-memory budget")
-    ap.add_argument("--max-active-particles", type=int, default=2_500_000,
+    ap.add_argument("--max-active-particles", type=int, default=3_500_000,
                     help="serving: admission stops above this many active particles")
     ap.add_argument("--plain-seconds", type=float, default=15.0,
                     help="serving: seconds of the one-request-at-a-time plain comparison")
+    ap.add_argument("--variant", choices=["fast", "exact"], default="fast",
+                    help="library build: fast (contracted arithmetic, within the stated tolerance of the "
+                         "oracle) or exact (bit-identical to the oracle)")
+    ap.add_argument("--served-seconds", type=float, default=12.0,
+                    help="batched run: seconds of the served leg (Poisson stream at --rate)")
+    ap.add_argument("--served-plain-seconds", type=float, default=8.0,
+                    help="batched run: seconds of the served leg's plain comparison")
+    ap.add_argument("--no-served", action="store_true", help="skip the served leg")
+    ap.add_argument("--tile-loads", choices=["tma", "cp_async"], default="tma",
+                    help="how the grid kernel stages its tiles (same results)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs")
+    ap.add_argument("--no-exact-build", action="store_true",
+                    help="skip timing the exact build beside the fast one")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    os.environ["VT_VARIANT"] = args.variant  # read when velvet_gb300 is first imported
     if args.impl == "reference":
         run_reference(args)
         return
@@ -685,6 +744,10 @@ def main() -> None:
         import velvet_gb300 as vg
 
         vg._abi.check(vg.lib().vt_tuning_set_grid_tile(args.grid_tile), "vt_tuning_set_grid_tile")
+    if args.tile_loads != "tma":
+        import velvet_gb300 as vg
+
+        vg._abi.check(vg.lib().vt_tuning_set_tile_loads(0), "vt_tuning_set_tile_loads")
     if args.profile_frames:
         profile_frames(args)
         return
@@ -790,65 +853,75 @@ def main() -> None:
     # inside the timed region.  Each form runs on a freshly built batch over the same
     # frames as the device-resident loop (the cost of a frame changes as the cloths fall
     # onto their colliders), so the forms differ only in how the host drives them.
-    host_pos = [torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
-    host_nrm = [torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
-    sh = vg.stream_handle(stream)
-    copy_stream = torch.cuda.Stream()
-    ch = vg.stream_handle(copy_stream)
-    copied = [torch.cuda.Event(), torch.cuda.Event()]
+    e2e = None
+    if not args.no_e2e:
+        host_pos = [torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+        host_nrm = [torch.empty((n_tot, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+        sh = vg.stream_handle(stream)
+        copy_stream = torch.cuda.Stream()
+        ch = vg.stream_handle(copy_stream)
+        copied = [torch.cuda.Event(), torch.cuda.Event()]
 
-    def e2e_step(b, f):
-        batch_frame(wl, b, f, stream, upload_colliders=True)
-        _abi.check(vg.lib().vt_batch_all_get(b.handle, 0, host_pos[0].data_ptr(), 1, sh), "all_get")
-        _abi.check(vg.lib().vt_batch_all_get(b.handle, 1, host_nrm[0].data_ptr(), 1, sh), "all_get")
+        def e2e_step(b, f):
+            batch_frame(wl, b, f, stream, upload_colliders=True)
+            _abi.check(vg.lib().vt_batch_all_get(b.handle, 0, host_pos[0].data_ptr(), 1, sh), "all_get")
+            _abi.check(vg.lib().vt_batch_all_get(b.handle, 1, host_nrm[0].data_ptr(), 1, sh), "all_get")
+            stream.synchronize()
+
+        host_enqueue_s = [0.0]
+
+        def e2e_pipelined(b, f):
+            t = time.perf_counter()
+            batch_frame(wl, b, f, stream, upload_colliders=True)
+            _abi.check(vg.lib().vt_batch_all_get_async(b.handle, 0, host_pos[f % 2].data_ptr(), ch), "all_get_async")
+            _abi.check(vg.lib().vt_batch_all_get_async(b.handle, 1, host_nrm[f % 2].data_ptr(), ch), "all_get_async")
+            copied[f % 2].record(copy_stream)
+            host_enqueue_s[0] += time.perf_counter() - t
+            if f > 0:
+                copied[(f - 1) % 2].synchronize()  # frame f-1 is in host memory
+
+        e2e_steps = args.steps
+        batch = build_batch(wl)
+        for f in range(args.warmup):
+            e2e_step(batch, f)
+        dist_sync()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            e2e_step(batch, args.warmup + k)
+        e2e_sync_s = max_over_ranks(time.perf_counter() - t0)
+        batch.close()
+        batch = build_batch(wl)
+        for f in range(args.warmup):
+            e2e_pipelined(batch, f)
+        copy_stream.synchronize()
+        dist_sync()
+        host_enqueue_s[0] = 0.0
+        e_first, e_last = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e2e_clocks = ClockSampler(local, pci)
+        t0 = time.perf_counter()
+        e_first.record(stream)
+        for k in range(e2e_steps):
+            e2e_pipelined(batch, args.warmup + k)
+        e_last.record(stream)
+        copy_stream.synchronize()
         stream.synchronize()
-
-    host_enqueue_s = [0.0]
-
-    def e2e_pipelined(b, f):
-        t = time.perf_counter()
-        batch_frame(wl, b, f, stream, upload_colliders=True)
-        _abi.check(vg.lib().vt_batch_all_get_async(b.handle, 0, host_pos[f % 2].data_ptr(), ch), "all_get_async")
-        _abi.check(vg.lib().vt_batch_all_get_async(b.handle, 1, host_nrm[f % 2].data_ptr(), ch), "all_get_async")
-        copied[f % 2].record(copy_stream)
-        host_enqueue_s[0] += time.perf_counter() - t
-        if f > 0:
-            copied[(f - 1) % 2].synchronize()  # frame f-1 is in host memory
-
-    e2e_steps = args.steps
-    batch = build_batch(wl)
-    for f in range(args.warmup):
-        e2e_step(batch, f)
-    dist_sync()
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
-        e2e_step(batch, args.warmup + k)
-    e2e_sync_s = max_over_ranks(time.perf_counter() - t0)
-    batch.close()
-    batch = build_batch(wl)
-    for f in range(args.warmup):
-        e2e_pipelined(batch, f)
-    copy_stream.synchronize()
-    dist_sync()
-    host_enqueue_s[0] = 0.0
-    e_first, e_last = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e2e_clocks = ClockSampler(local, pci)
-    t0 = time.perf_counter()
-    e_first.record(stream)
-    for k in range(e2e_steps):
-        e2e_pipelined(batch, args.warmup + k)
-    e_last.record(stream)
-    copy_stream.synchronize()
-    stream.synchronize()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_clock_info = e2e_clocks.stop()
-    e2e_device_ms = e_first.elapsed_time(e_last) / e2e_steps
-    e2e_value = job_pits * e2e_steps / e2e_s
-    e2e_sync_value = job_pits * e2e_steps / e2e_sync_s
-    ncol = sum(len(c.colliders(0)) for c in wl.cloths)
-    h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
-    d2h = n_tot * 24
-    batch.close()
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
+        e2e_clock_info = e2e_clocks.stop()
+        e2e_device_ms = e_first.elapsed_time(e_last) / e2e_steps
+        e2e_value = job_pits * e2e_steps / e2e_s
+        e2e_sync_value = job_pits * e2e_steps / e2e_sync_s
+        ncol = sum(len(c.colliders(0)) for c in wl.cloths)
+        h2d = ncol * 208 + len(wl.cloths) * 128  # collider blocks + per-cloth parameter blocks
+        d2h = n_tot * 24
+        batch.close()
+        e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "mode": "pipelined: frame k+1 computes while frame k's positions and normals copy to pinned "
+                       "host memory (vt_batch_all_get_async); all copies inside the timed region",
+               "synchronous_value": e2e_sync_value, "steps": e2e_steps,
+               "wall_ms_per_frame": 1000.0 * e2e_s / e2e_steps,
+               "device_ms_per_frame": e2e_device_ms,
+               "host_enqueue_ms_per_frame": 1000.0 * host_enqueue_s[0] / e2e_steps,
+               "clocks": e2e_clock_info}
 
     # ---- the plain drop-in solver on the same workload, one cloth at a time
     plain = None
@@ -872,6 +945,34 @@ def main() -> None:
         for s, _, _ in solvers:
             s.close()
 
+    # the served form on a bounded Poisson stream, and its plain comparison (one GPU)
+    served = None
+    if rank == 0 and world == 1 and not args.no_served:
+        sv, sp = serving_legs(args, args.served_seconds, args.served_plain_seconds)
+        served = {**sv, "plain": sp, "served_over_plain": sv["value"] / sp["value"],
+                  "config": {"rate_per_s": args.rate, "duration_s": args.served_seconds,
+                             "side": "log-uniform [16, 512]", "frames": "uniform [30, 300]",
+                             "budget_gb": args.budget_gb, "max_active_particles": args.max_active_particles}}
+
+    # the exact build (bit-identical to the oracle) on the same batched frames, in a child
+    # process (the library is chosen per process)
+    exact = None
+    if rank == 0 and world == 1 and args.variant == "fast" and not args.no_exact_build:
+        r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--variant", "exact", "--workload", args.workload,
+                            "--steps", str(args.steps), "--warmup", str(args.warmup), "--no-plain",
+                            "--no-cpu-baseline", "--no-served", "--no-e2e", "--seed", str(args.seed)]
+                           + (["--grid-tile", str(args.grid_tile)] if args.grid_tile >= 0 else []),
+                           capture_output=True, text=True, timeout=900)
+        try:
+            ex = json.loads(r.stdout.strip().splitlines()[-1])
+            exact = {"value": ex["value"], "ms_per_step": ex["ms_per_step"], "p99_frame_ms": ex["p99_frame_ms"],
+                     "roofline_frac": (ex.get("roofline") or {}).get("frac"),
+                     "avg_iteration_ms": (ex.get("roofline") or {}).get("avg_iteration_ms"),
+                     "what": "libvelvet_gb300.so: bit-identical to the oracle (no contraction, IEEE division "
+                             "and square root)"}
+        except (ValueError, IndexError, KeyError):
+            exact = {"error": (r.stdout[-300:] + r.stderr[-300:])}
+
     # the CPU legs run once, at one GPU: at N > 1 the other ranks' GPUs would wait on them
     cpu, cpu_ref_solver, cpu_ref_solver_all = None, None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -886,6 +987,8 @@ def main() -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic grid cloths generated from the config (seeded), no dataset",
             "config": {"workload": wl.name, "form": "batched (one graph launch per frame for all cloths)",
+                       "library": f"libvelvet_gb300{'_fast' if args.variant == 'fast' else ''}.so",
+                       "tile_loads": args.tile_loads,
                        "cloths_per_gpu": len(wl.cloths), "particles_per_gpu": n_tot,
                        "substeps": wl.substeps, "iterations": wl.iterations,
                        "grid_tile": None if CSR_KERNELS else grid_tile,
@@ -896,19 +999,14 @@ def main() -> None:
             "plain": plain,
             "batched_over_plain": (value / plain["value"]) if plain else None,
             "clocks": clock_info,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "mode": "pipelined: frame k+1 computes while frame k's positions and normals copy to pinned "
-                            "host memory (vt_batch_all_get_async); all copies inside the timed region",
-                    "synchronous_value": e2e_sync_value, "steps": e2e_steps,
-                    "wall_ms_per_frame": 1000.0 * e2e_s / e2e_steps,
-                    "device_ms_per_frame": e2e_device_ms,
-                    "host_enqueue_ms_per_frame": 1000.0 * host_enqueue_s[0] / e2e_steps,
-                    "clocks": e2e_clock_info},
+            "e2e": e2e,
             "gpu_launches": launches_timed,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "cpu_reference_cpu_solver": cpu_ref_solver,
             "cpu_reference_cpu_solver_all_cores": cpu_ref_solver_all,
+            "served": served,
+            "exact_build": exact,
             "host": host_info(),
         }
         print(json.dumps(line), flush=True)

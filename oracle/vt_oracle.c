@@ -182,6 +182,10 @@ typedef struct vo_solver {
     VEC(float) bd_rest;
     vt_sdf_collider* col;
     uint32_t ncol;
+    /* 1: the constraint kernels' atomics land in reverse constraint order (another valid
+     * order of the reference's unordered atomics), for measuring how much the result
+     * depends on that order */
+    int reverse_sums;
     /* spatial hash (SpatialHashGPU.hpp:18-29) */
     float cell_spacing;
     int32_t table_size;
@@ -243,6 +247,9 @@ VO_API void vo_set_params(vo_solver* s, const vt_params* P)
     s->P.num_particles = n;
 }
 VO_API uint32_t vo_num_particles(const vo_solver* s) { return s->n; }
+/* Sum order of the stretch, attachment and bending corrections: 0 constraint order (the
+ * default, the CUDA solver's order), 1 reverse constraint order. */
+VO_API void vo_set_sum_order(vo_solver* s, int reversed) { s->reverse_sums = reversed != 0; }
 VO_API int32_t vo_table_size(const vo_solver* s) { return s->table_size; }
 
 /* ------------------------------------------------------------------ registration */
@@ -634,7 +641,8 @@ static inline void add_delta(vo_solver* s, uint32_t i, v3 c)
 static void solve_stretch(vo_solver* s)
 {
     const v3* p = s->p.d;
-    for (size_t c = 0; c < s->st_rest.n; ++c) {
+    for (size_t k = 0; k < s->st_rest.n; ++k) {
+        const size_t c = s->reverse_sums ? s->st_rest.n - 1 - k : k;
         int i1 = s->st_idx.d[2 * c], i2 = s->st_idx.d[2 * c + 1];
         float rest = s->st_rest.d[c];
         v3 diff = vsub(p[i1], p[i2]);
@@ -656,7 +664,8 @@ static void solve_stretch(vo_solver* s)
 /* SolveAttachment_Kernel, :205-235 */
 static void solve_attach(vo_solver* s)
 {
-    for (size_t c = 0; c < s->at_pid.n; ++c) {
+    for (size_t k = 0; k < s->at_pid.n; ++k) {
+        const size_t c = s->reverse_sums ? s->at_pid.n - 1 - k : k;
         uint32_t pid = (uint32_t)s->at_pid.d[c];
         v3 slot = s->slots.d[s->at_slot.d[c]];
         float target = s->at_dist.d[c] * s->P.long_range_stretchiness;
@@ -675,7 +684,8 @@ static void solve_attach(vo_solver* s)
 static void solve_bending(vo_solver* s, float dt)
 {
     const v3* P = s->p.d;
-    for (size_t c = 0; c < s->bd_rest.n; ++c) {
+    for (size_t k = 0; k < s->bd_rest.n; ++k) {
+        const size_t c = s->reverse_sums ? s->bd_rest.n - 1 - k : k;
         uint32_t i0 = s->bd_idx.d[4 * c], i1 = s->bd_idx.d[4 * c + 1];
         uint32_t i2 = s->bd_idx.d[4 * c + 2], i3 = s->bd_idx.d[4 * c + 3];
         float rest = s->bd_rest.d[c];

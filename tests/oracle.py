@@ -52,6 +52,7 @@ def lib() -> C.CDLL:
             "vo_get_params": (None, [P, C.POINTER(VtParams)]),
             "vo_set_params": (None, [P, C.POINTER(VtParams)]),
             "vo_num_particles": (C.c_uint32, [P]),
+            "vo_set_sum_order": (None, [P, C.c_int]),
             "vo_table_size": (C.c_int32, [P]),
             "vo_cloth_add": (C.c_int32, [P, P, C.c_uint32, P, C.c_uint32, P, C.c_float]),
             "vo_stretch_add": (None, [P, C.c_int32, C.c_int32, C.c_float]),
@@ -183,6 +184,11 @@ class Oracle:
     @property
     def num_particles(self) -> int:
         return lib().vo_num_particles(self.h)
+
+    def set_sum_order(self, reversed_: bool) -> None:
+        """Reverse constraint order for the Jacobi sums: another valid order of the
+        reference's unordered atomics."""
+        lib().vo_set_sum_order(self.h, 1 if reversed_ else 0)
 
     def table_size(self) -> int:
         return lib().vo_table_size(self.h)

@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 import velvet_gb300 as vg
+from velvet_gb300 import _abi
 from velvet_gb300 import workloads as W
 from oracle import Oracle
 
@@ -82,6 +83,7 @@ def test_batch_mixing_kernel_kinds_equals_each_cloth_alone():
         assert np.array_equal(bits(batch.velocities(k)), bits(o.velocities())), f"cloth {k} velocities"
 
 
+@pytest.mark.skipif(_abi.VARIANT == "fast", reason="bits of the oracle / host arithmetic: exact build only")
 def test_batch_matches_oracle_with_moving_collider():
     wl = mixed(3, seed=5)
     batch = vg.BatchSolver()

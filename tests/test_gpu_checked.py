@@ -19,6 +19,7 @@ def test_gpu_suite_passes_on_the_bounds_checked_build():
     assert lib.exists(), "the bounds-checked library is missing: run __graft_entry__.build()"
     env = dict(os.environ, VT_CHECKED="1")
     r = subprocess.run([sys.executable, "-m", "pytest", str(ROOT / "tests"), "-m", "gpu", "-q", "-x",
-                        "-p", "no:cacheprovider", "--ignore", str(Path(__file__))],
+                        "-p", "no:cacheprovider", "--ignore", str(Path(__file__)),
+                        "--ignore", str(Path(__file__).with_name("test_gpu_fast_build.py"))],
                        cwd=ROOT, env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-4000:] + r.stderr[-2000:]

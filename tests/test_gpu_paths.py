@@ -116,6 +116,46 @@ def test_every_grid_tile_shape_gives_the_same_bits(variant, side):
         vg.lib().vt_tuning_set_grid_tile(-1)
 
 
+@pytest.mark.parametrize("tma", [1, 0], ids=["tma", "cp_async"])
+@pytest.mark.parametrize("variant", [0, 2, 4])
+def test_tile_loads_by_tma_and_by_cp_async_give_the_oracle_bits(variant, tma):
+    """The tile kernel stages its halo, rests and positions with TMA bulk tensor copies
+    (default) or per-thread cp.async (vt_tuning_set_tile_loads): both give the oracle's
+    bits, for every tile shape, on a cloth with partial tiles, two cached LRA slots and
+    the finalizing iterations' position loads, and on a batch of cloths of several sizes."""
+    assert vg.lib().vt_tuning_set_tile_loads(tma) == 0
+    assert vg.lib().vt_tuning_set_grid_tile(variant) == 0
+    try:
+        spec = spec_of(45, 0.4)
+        o, g = Oracle(), vg.ClothSolver()
+        for s in (o, g):
+            W.build_plain(spec, s)
+        run_frames([o, g], spec, 3)
+        same(g.positions(), o.positions(), f"tile loads {tma}, shape {variant}")
+        same(g.velocities(), o.velocities(), f"tile loads {tma}, shape {variant} velocities")
+        wl = W.batched(5, frames=2, seed=9, lo=10, hi=70)
+        batch, alone = vg.BatchSolver(), []
+        for c in wl.cloths:
+            s = vg.ClothSolver()
+            W.build_plain(c, s)
+            batch.add(s)
+            s.close()
+            a = Oracle()
+            W.build_plain(c, a)
+            alone.append(a)
+        for f in range(wl.frames):
+            batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin)
+            for a, c in zip(alone, wl.cloths):
+                a.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                           wl.collision_margin, c.particle_diameter())
+        batch.sync()
+        for k, a in enumerate(alone):
+            same(batch.positions(k), a.positions(), f"tile loads {tma}, batch cloth {k}")
+    finally:
+        vg.lib().vt_tuning_set_grid_tile(-1)
+        vg.lib().vt_tuning_set_tile_loads(1)
+
+
 @pytest.mark.parametrize("variant", [-1, 1, 5])
 @pytest.mark.parametrize("n_slots", [5, 24])
 def test_many_lra_slots_recompute_their_rests(n_slots, variant):

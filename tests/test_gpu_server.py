@@ -236,3 +236,42 @@ def test_rejects_non_grid_and_oversize():
     with pytest.raises(vg.VtError) as e:
         srv.submit(big, 1)
     assert e.value.status == _abi.VT_ERR_CAPACITY
+
+
+def test_admission_stops_on_a_budget_above_16_gb():
+    """A 20 GiB budget with the particle cap off: 173 requests of 512 x 512 particles and
+    a small one fill the arena (45.5 M particles; the arena's neighbour lists alone pass
+    2^31 words, so the small request's list block starts beyond a 32-bit offset), the
+    next request waits for memory, and the small request's result equals the same cloth
+    alone."""
+    budget = 20 << 30
+    S, It = 2, 2
+    srv = vg.ClothServer(hbm_budget_bytes=budget, max_cloths=256, max_active_particles=0, substeps=S,
+                         iterations=It)
+    per = 472  # device bytes per arena particle
+    cap = (budget - 256 * 1860 - (1 << 20)) // per
+    big = W.ClothSpec(512, 0.02, W.horizontal_cloth(512, 0.02, 0.8), [0, 511], request(16).colliders)
+    n_big = cap // (512 * 512)
+    assert n_big * 512 * 512 > (1 << 31) // 64, "the arena should pass the old 32-bit list offset"
+    small = request(32, 0.45)
+    ids = [submit_described(srv, big, 3) for _ in range(n_big)]
+    rid_small = submit_described(srv, small, 3)
+    rid_wait = submit_described(srv, big, 3)
+    info = srv.tick()
+    admitted = info.admitted
+    for _ in range(3):  # uploads may spread admissions over ticks
+        if srv.poll(rid_small)[0] == _abi.REQ_ACTIVE:
+            break
+        info = srv.tick()
+        admitted += info.admitted
+    assert srv.poll(rid_small)[0] in (_abi.REQ_ACTIVE, _abi.REQ_DONE)
+    assert srv.poll(rid_wait)[0] == _abi.REQ_QUEUED, "the request beyond the budget should wait"
+    assert admitted == n_big + 1
+    assert srv.stats().bytes_in_use <= budget
+    for _ in range(20):
+        info = srv.tick()
+        if srv.poll(rid_small)[0] == _abi.REQ_DONE and srv.poll(ids[-1])[0] == _abi.REQ_DONE:
+            break
+    assert srv.poll(rid_small) == (_abi.REQ_DONE, 3)
+    assert np.array_equal(bits(srv.result(rid_small)), bits(alone(small, 3, S, It)))
+    srv.close()

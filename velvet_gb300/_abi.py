@@ -1,9 +1,10 @@
 """ctypes view of include/velvet_gb300.h.
 
-`lib()` loads velvet_gb300/libvelvet_gb300.so (built in-tree by velvet_gb300.build; with
-VT_CHECKED=1 in the environment, its bounds-checked build libvelvet_gb300_checked.so)
-and declares every entry point's signature.  There is no fallback: if the library is
-missing or fails to load, `lib()` raises.
+`lib()` loads velvet_gb300/libvelvet_gb300.so (built in-tree by velvet_gb300.build) and
+declares every entry point's signature.  VT_VARIANT in the environment picks another
+build of the same sources: `checked` (bounds-checked; VT_CHECKED=1 means the same) or
+`fast` (contracted arithmetic, results within the solver's stated tolerance of the exact
+build).  There is no fallback: if the library is missing or fails to load, `lib()` raises.
 """
 from __future__ import annotations
 
@@ -11,9 +12,13 @@ import ctypes as C
 import os
 from pathlib import Path
 
-# VT_CHECKED=1 loads the bounds-checked build of the same sources (see build.py)
-LIB_PATH = Path(__file__).resolve().parent / (
-    "libvelvet_gb300_checked.so" if os.environ.get("VT_CHECKED") == "1" else "libvelvet_gb300.so")
+# the build variant (see build.py): exact (default), checked or fast
+VARIANT = os.environ.get("VT_VARIANT") or ("checked" if os.environ.get("VT_CHECKED") == "1" else "exact")
+_LIB_NAMES = {"exact": "libvelvet_gb300.so", "checked": "libvelvet_gb300_checked.so",
+              "fast": "libvelvet_gb300_fast.so"}
+if VARIANT not in _LIB_NAMES:
+    raise ValueError(f"VT_VARIANT={VARIANT!r}: expected one of {sorted(_LIB_NAMES)}")
+LIB_PATH = Path(__file__).resolve().parent / _LIB_NAMES[VARIANT]
 
 VT_OK = 0
 VT_ERR_INVALID_ARGUMENT = -1
@@ -217,6 +222,7 @@ SIGNATURES: dict[str, tuple] = {
     "vt_server_result": (I32, [P, C.c_int64, P, U32]),
     "vt_server_stats_get": (I32, [P, C.POINTER(VtServerStats)]),
     "vt_tuning_set_grid_tile": (I32, [I32]),
+    "vt_tuning_set_tile_loads": (I32, [I32]),
     "vt_solver_grid_tile": (I32, [P, PI32]),
     "vt_batch_grid_tile": (I32, [P, PI32]),
     "vt_camera_look_at": (I32, [PF, PF, PF, PF]),

@@ -1,15 +1,28 @@
-"""Builds the solver library in-tree: velvet_gb300/libvelvet_gb300.so (sm_103a).
+"""Builds the solver library in-tree for sm_103a, in three variants of the same sources.
 
-Every .cu file under velvet_gb300/csrc is compiled in parallel by nvcc for
-sm_103a only, then linked into one shared library whose C ABI is
-include/velvet_gb300.h.  Flags that matter for results:
-  -fmad=false                 no multiply-add contraction in device code
+  exact    velvet_gb300/libvelvet_gb300.so          (the default library)
+  checked  velvet_gb300/libvelvet_gb300_checked.so  exact + -DVT_CHECKED=1
+  fast     velvet_gb300/libvelvet_gb300_fast.so     contracted arithmetic (see FAST_FLAGS)
+
+Every .cu file under velvet_gb300/csrc is compiled in parallel by nvcc for sm_103a only,
+then linked into one shared library whose C ABI is include/velvet_gb300.h.
+
+exact: flags that fix every FP32 result to the IEEE-rounded value of the operations as
+written, on the device and in host code alike:
+  -fmad=false                   no multiply-add contraction in device code
   -Xcompiler -ffp-contract=off  the same for host code (gcc on aarch64 contracts by default)
-so every FP32 result is the IEEE-rounded value of the operations as written.
-
-build(checked=True) makes libvelvet_gb300_checked.so from the same sources with
--DVT_CHECKED=1: data-dependent device indices are range-checked and a failure is reported
+checked: -DVT_CHECKED=1 range-checks data-dependent device indices; a failure is reported
 by the sync calls (the library the tests can load instead with VT_CHECKED=1).
+fast: the solver kernels are compiled as nvcc compiles by default (-fmad=true, so a
+multiply followed by an add may become one FMA, as in the reference's own build) plus
+approximate division and square root, with CUDA's acosf for the dihedral angle and
+reciprocals taken once per vector division (-DVT_FAST=1).  Results differ from the exact
+build in the last bits of each operation; the tests bound the difference by the
+solver's stated tolerance.  The spatial hash (vt_hash.cu), its allocation-free entry
+point and the device grid builder (vt_build.cu) keep the exact flags, so cell keys, sort
+order and neighbour lists of given positions, and a cloth built on the device, are
+bit-identical in every variant; threshold decisions inside the fast kernels use exact
+distances too (vt_math.cuh).  Host code keeps -ffp-contract=off.
 """
 from __future__ import annotations
 
@@ -23,16 +36,27 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
-OUT = PKG / "libvelvet_gb300.so"
-OBJ = PKG / "_build"
-OUT_CHECKED = PKG / "libvelvet_gb300_checked.so"
-OBJ_CHECKED = PKG / "_build_checked"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = [
-    "-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-constexpr",
+COMMON_FLAGS = [
+    "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", str(INCLUDE),
 ]
+EXACT_FLAGS = ["-fmad=false"]
+FAST_FLAGS = ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-DVT_FAST=1"]
+# sources compiled with the exact flags in every variant (bit-identical hashing)
+EXACT_ONLY = {"vt_hash.cu", "vt_hash_noalloc.cu", "vt_build.cu"}
+
+VARIANTS = {
+    "exact": ("libvelvet_gb300.so", "_build", []),
+    "checked": ("libvelvet_gb300_checked.so", "_build_checked", ["-DVT_CHECKED=1"]),
+    "fast": ("libvelvet_gb300_fast.so", "_build_fast", None),
+}
+OUT = PKG / VARIANTS["exact"][0]
+
+
+def library_path(variant: str = "exact") -> Path:
+    return PKG / VARIANTS[variant][0]
 
 
 def nvcc() -> str:
@@ -42,14 +66,21 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build velvet_gb300")
 
 
-def _compile(src: Path, verbose_ptxas: bool, checked: bool = False) -> Path:
-    obj = (OBJ_CHECKED if checked else OBJ) / (src.stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *(["-DVT_CHECKED=1"] if checked else []), "-c", str(src), "-o", str(obj)]
+def flags_for(src: Path, variant: str) -> list[str]:
+    extra = VARIANTS[variant][2]
+    if extra is None:  # fast
+        return list(EXACT_FLAGS if src.name in EXACT_ONLY else FAST_FLAGS)
+    return [*EXACT_FLAGS, *extra]
+
+
+def _compile(src: Path, variant: str, verbose_ptxas: bool) -> Path:
+    obj = PKG / VARIANTS[variant][1] / (src.stem + ".o")
+    cmd = [nvcc(), *ARCH, *COMMON_FLAGS, *flags_for(src, variant), "-c", str(src), "-o", str(obj)]
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
+        raise RuntimeError(f"nvcc failed on {src.name} ({variant}):\n{r.stdout}\n{r.stderr}")
     if verbose_ptxas:
         sys.stderr.write(r.stderr)
     return obj
@@ -67,15 +98,17 @@ def up_to_date(out: Path = OUT) -> bool:
     return all(p.stat().st_mtime <= t for p in deps)
 
 
-def build(force: bool = False, verbose_ptxas: bool = False, checked: bool = False) -> Path:
-    """Compiles and links the library (or its bounds-checked twin) if any source is newer."""
-    out, obj_dir = (OUT_CHECKED, OBJ_CHECKED) if checked else (OUT, OBJ)
+def build(force: bool = False, verbose_ptxas: bool = False, checked: bool = False,
+          variant: str | None = None) -> Path:
+    """Compiles and links one variant of the library if any source is newer."""
+    variant = variant or ("checked" if checked else "exact")
+    out, obj_dir = PKG / VARIANTS[variant][0], PKG / VARIANTS[variant][1]
     if not force and up_to_date(out):
         return out
     obj_dir.mkdir(exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas, checked), srcs))
+        objs = list(ex.map(lambda s: _compile(s, variant, verbose_ptxas), srcs))
     tmp = out.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -86,4 +119,6 @@ def build(force: bool = False, verbose_ptxas: bool = False, checked: bool = Fals
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv, checked="--checked" in sys.argv))
+    v = next((a.split("=", 1)[1] for a in sys.argv if a.startswith("--variant=")),
+             "checked" if "--checked" in sys.argv else "exact")
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv, variant=v))

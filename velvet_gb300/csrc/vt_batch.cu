@@ -218,6 +218,10 @@ vt_status vt_batch_sync(vt_batch* b)
             vt::set_error("a device-side bounds check failed (bounds-checked build)");
             return VT_ERR_STATE;
         }
+        if (flags[0] & vt::VT_STATUS_TIMEOUT) {
+            vt::set_error("a device-side bounded wait gave up (tile loads did not arrive)");
+            return VT_ERR_TIMEOUT;
+        }
         vt::set_error("non-finite particle state detected on the device");
         return VT_ERR_NUMERIC;
     }

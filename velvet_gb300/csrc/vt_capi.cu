@@ -567,6 +567,10 @@ vt_status vt_solver_sync(vt_solver* s)
             vt::set_error("a device-side bounds check failed (bounds-checked build)");
             return VT_ERR_STATE;
         }
+        if (flags[0] & vt::VT_STATUS_TIMEOUT) {
+            vt::set_error("a device-side bounded wait gave up (tile loads did not arrive)");
+            return VT_ERR_TIMEOUT;
+        }
         vt::set_error("non-finite particle state detected on the device");
         return VT_ERR_NUMERIC;
     }
@@ -790,6 +794,24 @@ vt_status vt_solver_debug_get(vt_solver* s, int32_t what, void* dst, uint64_t by
         if (n) VT_TRY_CUDA(cudaMemcpy2D(dst, 12, d.p[s->world.pcur], 16, 12, n, cudaMemcpyDeviceToHost), "copy");
         return VT_OK;
     }
+    if (what == VT_DEBUG_NEIGHBORS && n) {
+        // the device keeps the lists in sorted-slot order (column t = the particle in
+        // sorted slot t); the reference's layout puts particle id's list in column id
+        VT_GUARD_BEGIN
+        const uint64_t mn = (uint64_t)s->h.P.max_num_neighbors;
+        std::vector<uint32_t> lists(n * mn), order(n);
+        VT_TRY_CUDA(cudaMemcpy(lists.data(), d.nbr, 4 * n * mn, cudaMemcpyDeviceToHost), "copy");
+        VT_TRY_CUDA(cudaMemcpy(order.data(), d.vals, 4 * n, cudaMemcpyDeviceToHost), "copy");
+        uint32_t* out = static_cast<uint32_t*>(dst);
+        std::memset(out, 0xff, 4 * n * mn);
+        for (uint64_t t = 0; t < n; ++t) {
+            const uint64_t id = order[t];
+            if (id >= n) continue;
+            for (uint64_t k = 0; k < mn; ++k) out[id + k * n] = lists[t + k * n];
+        }
+        return VT_OK;
+        VT_GUARD_END
+    }
     if (need) VT_TRY_CUDA(cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost), "copy");
     return VT_OK;
 }
@@ -821,6 +843,7 @@ vt_status vt_solver_use_grid_kernel(vt_solver* s, int32_t on)
 }
 
 vt_status vt_tuning_set_grid_tile(int32_t variant) { return vt::tuning_force(variant); }
+vt_status vt_tuning_set_tile_loads(int32_t tma) { return vt::set_tile_loads_tma(tma != 0); }
 
 vt_status vt_solver_grid_tile(const vt_solver* s, int32_t* variant)
 {

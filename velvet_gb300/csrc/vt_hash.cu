@@ -385,25 +385,30 @@ __device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* 
 // The same walk over sorted-slot copies of the positions: candidate k is ps[k] (its
 // position, its index in w) and x0s[k], one 16-byte load each, contiguous within a
 // bucket; the thread's own object is slot t, so the threads of a warp share buckets.
-// Same arithmetic, order and caps.  (Measured alternatives: threads in object order, a
-// warp per object, a warp per cell group, and (start, end) pairs loaded three buckets
-// at a time all ran slower — the walk is bound by load latency, and sorted order with
-// the highest occupancy gives the most shared bucket reads.)
+// Same arithmetic, order and caps.  The list is written in sorted-slot order (column
+// t - slot_base of the domain's block), so a warp's stores of entry k are consecutive
+// words; the collision pass reads the lists in the same order.  (Measured alternatives:
+// threads in object order, a warp per object, a warp per cell group, and (start, end)
+// pairs loaded three buckets at a time all ran slower — the walk is bound by load
+// latency, and sorted order with the highest occupancy gives the most shared bucket
+// reads.)
 __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint32_t* __restrict__ cs,
                                                        const uint32_t* __restrict__ ce,
                                                        const float4* __restrict__ ps,
                                                        const float4* __restrict__ x0s,
                                                        uint32_t* __restrict__ out_base, uint32_t id_base,
-                                                       int32_t n, int32_t table_base, int32_t table,
-                                                       uint64_t M, float sp, float sp2, float diam2,
-                                                       int32_t max_nbr, uint32_t slot_end, int32_t* status)
+                                                       uint32_t slot_base, int32_t n, int32_t table_base,
+                                                       int32_t table, uint64_t M, float sp, float sp2,
+                                                       float diam2, int32_t max_nbr, uint32_t slot_end,
+                                                       int32_t* status)
 {
     const float4 own = ps[t];
     const uint32_t id = __float_as_uint(own.w);
     const vec3 position = xyz(own);
     const int32_t ix = int_coord(position.x, sp), iy = int_coord(position.y, sp),
                   iz = int_coord(position.z, sp);
-    uint32_t* out = out_base + (id - id_base);
+    if (!VT_IN_RANGE(t, slot_base, (long long)slot_base + n, status)) return;
+    uint32_t* out = out_base + (t - slot_base);
     // the 27 keys are XORs of per-axis products: (x+dx)*A etc. wrap like x*A
     uint32_t hx[3], hy[3], hz[3];
 #pragma unroll
@@ -470,9 +475,10 @@ k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict
     if (t >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
     // a domain's sorted slots are its particle range
-    cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + D.nbr_base, (uint32_t)D.p_begin, D.p_count,
-                           D.table_base, D.table_size, ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing,
-                           D.cell_spacing2, D.diameter2, D.max_nbr, (uint32_t)(D.p_begin + D.p_count), status);
+    cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + nbr_offset(D), (uint32_t)D.p_begin,
+                           (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
+                           ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2, D.diameter2,
+                           D.max_nbr, (uint32_t)(D.p_begin + D.p_count), status);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -513,11 +519,14 @@ k_hash_keys_arena(const int32_t* __restrict__ pdom, const DomainParams* __restri
     vals[i] = (uint32_t)i;
 }
 
+// Cell ranges and sorted copies as k_cell_ranges_gather, plus each domain's first sorted
+// slot: a domain's keys form one contiguous run of the sorted order, so the slot where
+// the domain of vals[t] differs from that of vals[t - 1] starts it.
 __global__ void __launch_bounds__(kBlock)
 k_cell_ranges_arena(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                    const float4* __restrict__ p, const float4* __restrict__ x0, int32_t n, uint32_t sentinel,
-                    uint32_t* __restrict__ cs, uint32_t* __restrict__ ce, float4* __restrict__ ps,
-                    float4* __restrict__ x0s)
+                    const int32_t* __restrict__ pdom, const float4* __restrict__ p, const float4* __restrict__ x0,
+                    int32_t n, uint32_t sentinel, uint32_t* __restrict__ cs, uint32_t* __restrict__ ce,
+                    float4* __restrict__ ps, float4* __restrict__ x0s, int32_t* __restrict__ dslot)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
     if (t >= n) return;
@@ -529,6 +538,8 @@ k_cell_ranges_arena(const uint32_t* __restrict__ keys, const uint32_t* __restric
     }
     if (t == n - 1 || keys[t + 1] == sentinel) ce[h] = (uint32_t)(t + 1);
     const uint32_t id = vals[t];
+    const int32_t dom = pdom[id];
+    if (t == 0 || pdom[vals[t - 1]] != dom) dslot[dom] = t;
     const float4 q = p[id];
     ps[t] = make_float4(q.x, q.y, q.z, __uint_as_float(id));
     x0s[t] = x0[id];
@@ -538,14 +549,16 @@ __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors_arena(const int32_t* __restrict__ pdom, const DomainParams* __restrict__ doms,
                         const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
                         const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
-                        int32_t n_active, int32_t* __restrict__ status)
+                        const int32_t* __restrict__ dslot, int32_t n_active, int32_t* __restrict__ status)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
     if (t >= n_active) return;
-    const DomainParams& D = doms[pdom[__float_as_uint(ps[t].w)]];
-    cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + D.nbr_base, (uint32_t)D.p_begin, D.p_count,
-                           D.table_base, D.table_size, ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing,
-                           D.cell_spacing2, D.diameter2, D.max_nbr, (uint32_t)n_active, status);
+    const int32_t dom = pdom[__float_as_uint(ps[t].w)];
+    const DomainParams& D = doms[dom];
+    cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + nbr_offset(D), (uint32_t)D.p_begin,
+                           (uint32_t)dslot[dom], D.p_count, D.table_base, D.table_size,
+                           ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2, D.diameter2,
+                           D.max_nbr, (uint32_t)n_active, status);
 }
 
 cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pin, int32_t hw,
@@ -559,11 +572,11 @@ cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pi
     k_hash_keys_arena<<<blocks, kBlock, 0, st>>>(pdom, d.dom, d.p[pin], d.keys, d.vals, hw, sentinel);
     e = radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot, hw, bits, st, d.status);
     if (e != cudaSuccess) return e;
-    k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, d.vals, d.p[pin], d.x0, hw, sentinel, d.cell_start,
-                                                   d.cell_end, d.ps, d.x0s);
+    k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, d.vals, pdom, d.p[pin], d.x0, hw, sentinel,
+                                                   d.cell_start, d.cell_end, d.ps, d.x0s, d.dslot);
     if (n_active > 0)
         k_cache_neighbors_arena<<<(n_active + kBlock - 1) / kBlock, kBlock, 0, st>>>(
-            pdom, d.dom, d.cell_start, d.cell_end, d.ps, d.x0s, d.nbr, n_active, d.status);
+            pdom, d.dom, d.cell_start, d.cell_end, d.ps, d.x0s, d.nbr, d.dslot, n_active, d.status);
     const int passes = (hw > 1 && bits > 0) ? (bits + 7) / 8 : 0;
     if (launches) *launches += 3 + 3 * (uint64_t)passes;
     return cudaGetLastError();

@@ -19,7 +19,7 @@
 //     substep's PredictPositions are fused into the last iteration's gather; the
 //     pre-stabilisation CollideSDF is fused with the first PredictPositions.
 //   * float4 particles (w = inverse mass) so each particle is one 16-byte load.
-// Also here: the device grid builder (k_grid_build) and read-back packing (k_pack_xyz).
+// Also here: read-back packing (k_pack_xyz).  The device grid builder is in vt_build.cu.
 #include <utility>
 
 #include "vt_math.cuh"
@@ -47,6 +47,56 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
+// ------------------------------------------------------------------ TMA + mbarrier
+// The tile kernel's bulk tensor loads: one thread arms a shared-memory mbarrier with the
+// bytes it expects and issues cp.async.bulk.tensor copies of the halo tile and the other
+// per-tile arrays; every thread then waits on the barrier's phase 0 (bounded, see
+// mbar_wait).  Coordinates are (component 0, column, row) of a map from tmap_index.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.b32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for phase `phase` of the barrier; gives up after kMbarTries attempts (each
+// attempt may suspend the thread for a short, hardware-chosen time) and returns false.
+constexpr int kMbarTries = 1 << 20;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
+{
+    for (int k = 0; k < kMbarTries; ++k)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // ------------------------------------------------------------------ colliders
 __device__ __forceinline__ float sgnf(float v) { return (v > 0) ? 1.0f : (v < 0 ? -1.0f : 0.0f); }
 
@@ -65,11 +115,11 @@ __device__ vec3 collider_sdf(const ColliderDev& c, vec3 t, float margin)
     } else if (c.type == 0) {  // sphere
         float radius = c.sx + margin;
         vec3 diff = t - mk3(c.px, c.py, c.pz);
-        const float q = dot(diff, diff);
+        const float q = dot_exact(diff, diff);
         // outside for sure (no square root): q >= RN(RN(r*r) * (1 + 2^-20)) > r^2 gives
         // RN(sqrt(q)) >= r, so offset >= 0, whatever the rounding (r kept in the normal range)
         if (radius > 1e-18f && radius < 1e18f && q >= (radius * radius) * kFarMargin) return mk3(0, 0, 0);
-        float distance = sqrtf(q);
+        float distance = sqrt_exact(q);
         float offset = distance - radius;
         if (offset < 0) {
             vec3 direction = diff / distance;
@@ -179,17 +229,28 @@ k_presdf_predict(const Tile* __restrict__ tiles, const DomainParams* __restrict_
 
 // ------------------------------------------------------------------ collide particles + SDF
 // CollideParticles_Kernel (VtClothSolverGPU.cu:329-373) + ApplyDeltas (:253-264) +
-// CollideSDF (:289-314) for one substep.
+// CollideSDF (:289-314) for one substep.  With self-collision the threads take the
+// domain's particles in sorted-slot order (thread r of the domain: the particle in its
+// r-th sorted slot), so each thread's neighbour list is column r and a warp reads entry
+// k of 32 lists as consecutive words; a particle's result does not depend on which
+// thread computes it.
 __global__ void __launch_bounds__(kBlock)
 k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
           const ColliderDev* __restrict__ cols, const float4* __restrict__ x,
           const float4* __restrict__ pin, float4* __restrict__ pout,
-          const uint32_t* __restrict__ nbr, int32_t* __restrict__ status)
+          const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ vals,
+          const int32_t* __restrict__ dslot, int32_t* __restrict__ status)
 {
     const Tile tl = tiles[blockIdx.x];
-    const int i = tl.begin + (int)threadIdx.x;
-    if (i >= tl.end) return;
+    const int t = tl.begin + (int)threadIdx.x;
+    if (t >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
+    const int r = t - D.p_begin;  // rank within the domain
+    int i = t;
+    if (D.self_collision) {
+        i = (int)vals[(dslot ? dslot[tl.dom] : D.p_begin) + r];
+        if (!VT_IN_RANGE(i, D.p_begin, D.p_begin + D.p_count, status)) return;
+    }
     const float4 pi4 = pin[i];
     vec3 pi = xyz(pi4);
     const float wi = pi4.w;
@@ -198,7 +259,7 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
         vec3 delta = mk3(0, 0, 0);
         int count = 0;
         const vec3 veli = pi - xi;
-        const uint32_t* nb = nbr + D.nbr_base + (i - D.p_begin);
+        const uint32_t* nb = nbr + nbr_offset(D) + r;
         const int stride = D.p_count;
         const float diam = D.diameter;
         const bool far_ok = diam > 1e-18f && diam < 1e18f;
@@ -228,9 +289,9 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
                 if (denom <= 0) continue;
                 const vec3 pj = xyz(pj4);
                 const vec3 diff = pi - pj;
-                const float q = dot(diff, diff);
+                const float q = dot_exact(diff, diff);
                 if (far_ok && q >= far2) continue;  // d >= diam without the square root
-                const float d = sqrtf(q);
+                const float d = sqrt_exact(q);
                 if (d >= diam) continue;
                 const vec3 grad = diff / (d + VT_EPSILON);
                 const float lambda = (d - diam) / denom;
@@ -266,26 +327,27 @@ __device__ __forceinline__ void bend_eval(float4 a0, float4 a1, float4 a2, float
     c2 = c0;
     c3 = c0;
     const vec3 e = p3 - p2;
-    const float elen = length(e);
+    const float elen = length_exact(e);
     if (elen < VT_EPSILON) return;
     const float inv = 1.0f / elen;
-    vec3 n1 = cross(p2 - p0, p3 - p0);
-    n1 = n1 / dot(n1, n1);
-    vec3 n2 = cross(p3 - p1, p2 - p1);
-    n2 = n2 / dot(n2, n2);
+    // the angle chain in exact operations (vt_math.cuh: acos near a flat pair)
+    vec3 n1 = cross_exact(p2 - p0, p3 - p0);
+    n1 = div_exact(n1, dot_exact(n1, n1));
+    vec3 n2 = cross_exact(p3 - p1, p2 - p1);
+    n2 = div_exact(n2, dot_exact(n2, n2));
     const vec3 d0 = n1 * elen;
     const vec3 d1 = n2 * elen;
     const vec3 d2 = n1 * (dot(p0 - p3, e) * inv) + n2 * (dot(p1 - p3, e) * inv);
     const vec3 d3 = n1 * (dot(p2 - p0, e) * inv) + n2 * (dot(p2 - p1, e) * inv);
-    n1 = normalize(n1);
-    n2 = normalize(n2);
-    const float phi = vt_acosf(gclamp(dot(n1, n2), -1.0f, 1.0f));
+    n1 = normalize_exact(n1);
+    n2 = normalize_exact(n2);
+    const float phi = vt_acosf_exact(gclamp(dot_exact(n1, n2), -1.0f, 1.0f));
     float lambda = w0 * dot(d0, d0) + w1 * dot(d1, d1);
     lambda = lambda + w2 * dot(d2, d2);
     lambda = lambda + w3 * dot(d3, d3);
     if (lambda < VT_EPSILON) return;
     lambda = (phi - rest) / (lambda + xpbd);
-    if (dot(cross(n1, n2), e) > 0.0f) lambda = -lambda;
+    if (dot_exact(cross_exact(n1, n2), e) > 0.0f) lambda = -lambda;
     const vec3 k0 = d0 * (-w0 * lambda), k1 = d1 * (-w1 * lambda);
     const vec3 k2 = d2 * (-w2 * lambda), k3 = d3 * (-w3 * lambda);
     c0 = make_float4(k0.x, k0.y, k0.z, 1.0f);
@@ -302,7 +364,7 @@ __device__ __forceinline__ void bend_eval(float4 a0, float4 a1, float4 a2, float
 __device__ __forceinline__ bool stretch_common(float4 pa, float4 pb, float rest, vec3& common)
 {
     const vec3 diff = xyz(pa) - xyz(pb);
-    const float d = length(diff);
+    const float d = length_exact(diff);
     const float denom = pa.w + pb.w;
     if (!(d != rest && denom > 0)) return false;
     const vec3 grad = diff / (d + VT_EPSILON);
@@ -316,7 +378,7 @@ __device__ __forceinline__ void attach_one(vec3 pi, float wi, vec3 slot, float t
 {
     if (wi == 0 && target > 0) return;
     const vec3 diff = pi - slot;
-    const float d = length(diff);
+    const float d = length_exact(diff);
     if (d > target) {
         acc3(acc, (-diff) + (diff / d) * target);
         cnt++;
@@ -339,9 +401,9 @@ __device__ __forceinline__ void attach_one_filtered(vec3 pi, float wi, vec3 slot
 {
     if (wi != 0.0f && target > 1e-18f && target < 1e18f) {
         const vec3 diff = pi - slot;
-        const float q = dot(diff, diff);
+        const float q = dot_exact(diff, diff);
         if (q < (target * target) * kAttachMargin) return;
-        const float d = sqrtf(q);
+        const float d = sqrt_exact(q);
         if (d > target) {
             acc3(acc, (-diff) + (diff / d) * target);
             cnt++;
@@ -360,13 +422,13 @@ __device__ __forceinline__ void attach_lra_filtered(vec3 pi, float wi, vec3 slot
                                                     float c2, vec3& acc, int& cnt)
 {
     const vec3 r = slot0 - x0i;
-    const float q0 = dot(r, r);
+    const float q0 = dot_exact(r, r);
     if (wi != 0.0f && q0 > 1e-20f && q0 < 1e20f && lrs > 1e-4f && lrs < 1e4f) {
         const vec3 diff = pi - slot;
-        const float q = dot(diff, diff);
+        const float q = dot_exact(diff, diff);
         if (q < q0 * c2) return;
     }
-    attach_one(pi, wi, slot, sqrtf(q0) * lrs, acc, cnt);
+    attach_one(pi, wi, slot, sqrt_exact(q0) * lrs, acc, cnt);
 }
 
 // Groups of LRA slots (cloths with more slots than the per-particle cache): a whole group
@@ -485,7 +547,7 @@ __device__ __forceinline__ void apply_and_finalize(const DomainParams& D, int do
     const vec3 xi = xyz(x4);
     vec3 np = pi;
     vec3 rv = (np - xi) / dt;
-    const float rl = length(rv);
+    const float rl = length_exact(rv);
     if (rl > D.max_speed) {
         rv = (rv / rl) * D.max_speed;
         np = xi + rv * dt;
@@ -571,7 +633,7 @@ k_solve(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
             const LraGroup g = lra[-en.x - 1];
             const vec3 x0i = xyz(x0[i]);
             for (int s = g.slot_begin; s < g.slot_begin + g.slot_count; ++s) {
-                const float rest = length(xyz(slots0[s]) - x0i);
+                const float rest = length_exact(xyz(slots0[s]) - x0i);
                 attach_one(pi, wi, xyz(slots[s]), rest * lrs, acc, cnt);
             }
         }
@@ -629,23 +691,24 @@ __device__ __forceinline__ void bend_eval_grid(float4 a0, float4 a1, float4 a2, 
     const float elen = d3;
     if (elen < VT_EPSILON) return;
     const float inv = 1.0f / elen;
-    vec3 n1 = cross(p2 - p0, p3 - p0);
-    n1 = n1 / dot(n1, n1);
-    vec3 n2 = cross(p3 - p1, p2 - p1);
-    n2 = n2 / dot(n2, n2);
+    // the angle chain in exact operations (vt_math.cuh: acos near a flat pair)
+    vec3 n1 = cross_exact(p2 - p0, p3 - p0);
+    n1 = div_exact(n1, dot_exact(n1, n1));
+    vec3 n2 = cross_exact(p3 - p1, p2 - p1);
+    n2 = div_exact(n2, dot_exact(n2, n2));
     const vec3 d0 = n1 * elen;
     const vec3 d1 = n2 * elen;
     const vec3 d2 = n1 * (dot(p0 - p3, e) * inv) + n2 * (dot(p1 - p3, e) * inv);
     const vec3 dd3 = n1 * (dot(p2 - p0, e) * inv) + n2 * (dot(p2 - p1, e) * inv);
-    n1 = normalize(n1);
-    n2 = normalize(n2);
-    const float phi = vt_acosf(gclamp(dot(n1, n2), -1.0f, 1.0f));
+    n1 = normalize_exact(n1);
+    n2 = normalize_exact(n2);
+    const float phi = vt_acosf_exact(gclamp(dot_exact(n1, n2), -1.0f, 1.0f));
     float lambda = w0 * dot(d0, d0) + w1 * dot(d1, d1);
     lambda = lambda + w2 * dot(d2, d2);
     lambda = lambda + w3 * dot(dd3, dd3);
     if (lambda < VT_EPSILON) return;
     lambda = (phi - rest) / (lambda + xpbd);
-    if (dot(cross(n1, n2), e) > 0.0f) lambda = -lambda;
+    if (dot_exact(cross_exact(n1, n2), e) > 0.0f) lambda = -lambda;
     const vec3 k0 = d0 * (-w0 * lambda), k1 = d1 * (-w1 * lambda);
     const vec3 k2 = d2 * (-w2 * lambda), k3 = dd3 * (-w3 * lambda);
     c0 = make_float4(k0.x, k0.y, k0.z, 1.0f);
@@ -687,7 +750,7 @@ __device__ __forceinline__ void grid_generator(int X, int Y, int R, const float4
     if (full) {  // t3: (x,y+1)-(x+1,y); its length is the bend's shared-edge length
         const float4 a01 = sp[hx][hy + 1], a10 = sp[hx + 1][hy];
         const vec3 e3 = xyz(a01) - xyz(a10);
-        d3 = length(e3);
+        d3 = length_exact(e3);
         if (stretch_common_d(e3, d3, a01.w, a10.w, rest.w, cm)) r = make_float4(cm.x, cm.y, cm.z, 1.0f);
     }
     sst[3][gx][gy] = r;
@@ -788,19 +851,22 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
             const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ x,
             float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ grest,
             const float4* __restrict__ glra, const float4* __restrict__ slots,
-            const float4* __restrict__ slots0, int32_t* __restrict__ status)
+            const float4* __restrict__ slots0, int32_t* __restrict__ status,
+            const CUtensorMap* __restrict__ tmaps, int pin_sel)
 {
     constexpr int kGHA = kTA + 2, kGHB = kTB + 2;  // halo tile
     constexpr int kGGA = kTA + 1, kGGB = kTB + 1;  // generators, kGGA * kGGB == kBlock
     static_assert(kGGA * kGGB == kBlock, "one generator per thread");
-    __shared__ float4 sp[kGHA][kGHB];
-    __shared__ float4 sst[4][kGGA][kGGB];  // stretch common + fired flag, per type
+    // TMA destinations are 128-byte aligned
+    __shared__ __align__(128) float4 sp[kGHA][kGHB];
+    __shared__ __align__(128) float4 sst[4][kGGA][kGGB];  // stretch common + fired flag, per type
     // the generator's four stretch rest lengths are staged in sst[0] at the generator's own
     // slot (gx * kGGB + gy == tid): the thread reads them before it writes that slot
     float4* const sgr = &sst[0][0][0];
     __shared__ float4 sbd[4][kGGA][kGGB];  // bending corner corrections + fired flag
-    __shared__ float4 sgl[kBlock];         // the particle's LRA rest distances, or the slot groups' boxes
-    __shared__ float4 sx[kBlock];          // the particle's position (finalizing modes)
+    __shared__ __align__(128) float4 sgl[kBlock];  // the particle's LRA rest distances, or the slot groups' boxes
+    __shared__ __align__(128) float4 sx[kBlock];   // the particle's position (finalizing modes)
+    __shared__ __align__(8) uint64_t sbar;         // TMA completion barrier
     __shared__ float4 sslot[kGridLraCached];
     __shared__ float4 ssup[4 * (kLraGroupsMax / kLraSuper)];  // the slot super-groups' boxes
     __shared__ __align__(16) DomainParams sdom;
@@ -816,26 +882,66 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     const bool owns = tid < kTA * kTB && a < V && b < V;
     const int i = base + a * V + b;
 
-    // 1. stage with asynchronous copies (no registers held across the wait): the halo
-    // tile of predicted positions, each generator's rests, each particle's LRA rests and
-    // position, the LRA slots and the domain's parameters
-    for (int k = tid; k < kGHA * kGHB; k += kBlock) {
-        const int ha = k / kGHB, hb = k - ha * kGHB;
-        const int pa = a0 - 1 + ha, pb = b0 - 1 + hb;
-        const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V;
-        cp_async16_zfill(&sp[ha][hb], pin + (in ? base + pa * V + pb : base), in);
+    // 1. stage the halo tile of predicted positions, each generator's rests and each
+    // particle's LRA rests and position: with TMA, four bulk tensor copies (rectangles of
+    // the cloth's V x V grid, zero outside it) issued by one thread; otherwise one 16-byte
+    // cp.async per element with zero-fill outside the cloth.  Then the LRA slots and the
+    // domain's parameters (cp.async), and no registers held across the waits.
+    const bool tma = tmaps != nullptr;
+    const bool stage_lra = ns >= 1 && ns <= kGridLraCached;
+    if (tma) {
+        if (tid == 0) mbar_init(&sbar, 1);
+        __syncthreads();  // the barrier is initialised before anyone waits on it
+        if (tid == 0) {
+            const CUtensorMap* m = tmaps + tmap_index(tl.dom, tmap_shape_of(kTA), 0);
+            const uint32_t bytes = 16u * (uint32_t)(kGHA * kGHB + kGGA * kGGB + (stage_lra ? kTA * kTB : 0) +
+                                                   (kMode != SOLVE_PLAIN ? kTA * kTB : 0));
+            mbar_expect_tx(&sbar, bytes);
+            tma_load_3d(&sp[0][0], m + (pin_sel ? TMAP_P1 : TMAP_P0), 0, b0 - 1, a0 - 1, &sbar);
+            tma_load_3d(sgr, m + TMAP_GREST, 0, b0 - 1, a0 - 1, &sbar);
+            if (stage_lra) tma_load_3d(sgl, m + TMAP_GLRA, 0, b0, a0, &sbar);
+            if (kMode != SOLVE_PLAIN) tma_load_3d(sx, m + TMAP_X, 0, b0, a0, &sbar);
+        }
+    } else {
+        for (int k = tid; k < kGHA * kGHB; k += kBlock) {
+            const int ha = k / kGHB, hb = k - ha * kGHB;
+            const int pa = a0 - 1 + ha, pb = b0 - 1 + hb;
+            const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V;
+            cp_async16_zfill(&sp[ha][hb], pin + (in ? base + pa * V + pb : base), in);
+        }
+        {
+            const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
+            const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
+            cp_async16_zfill(&sgr[tid], grest + (gen ? base + X * V + Y : base), gen);
+        }
+        if (owns && stage_lra) cp_async16(&sgl[tid], glra + i);
+        if (kMode != SOLVE_PLAIN && owns) cp_async16(&sx[tid], x + i);
     }
-    {
-        const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
-        const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
-        cp_async16_zfill(&sgr[tid], grest + (gen ? base + X * V + Y : base), gen);
-    }
-    if (owns && ns >= 1 && ns <= kGridLraCached) cp_async16(&sgl[tid], glra + i);
-    if (kMode != SOLVE_PLAIN && owns) cp_async16(&sx[tid], x + i);
     if (tid < ns && tid < kGridLraCached) cp_async16(&sslot[tid], slots + s0 + tid);
     if (tid < (int)(sizeof(DomainParams) / 16))
         cp_async16(reinterpret_cast<float4*>(&sdom) + tid, reinterpret_cast<const float4*>(doms + tl.dom) + tid);
     cp_async_wait_all();
+    if (tma) {
+        // every thread waits for the copies; if any gave up, the block reports it and ends
+        const bool arrived = mbar_wait(&sbar, 0);
+        if (__syncthreads_or(!arrived)) {
+            if (tid == 0) atomicOr(status, VT_STATUS_TIMEOUT);
+            return;
+        }
+#if VT_CHECKED
+        // the bounds-checked build compares the staged halo with the global array
+        for (int k = tid; k < kGHA * kGHB; k += kBlock) {
+            const int ha = k / kGHB, hb = k - ha * kGHB;
+            const int pa = a0 - 1 + ha, pb = b0 - 1 + hb;
+            const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V;
+            const float4 want = in ? pin[base + pa * V + pb] : make_float4(0, 0, 0, 0);
+            const float4 got = sp[ha][hb];
+            if (__float_as_uint(got.x) != __float_as_uint(want.x) || __float_as_uint(got.y) != __float_as_uint(want.y) ||
+                __float_as_uint(got.z) != __float_as_uint(want.z) || __float_as_uint(got.w) != __float_as_uint(want.w))
+                atomicOr(status, VT_STATUS_BOUNDS);
+        }
+#endif
+    }
     __syncthreads();
     const DomainParams& D = sdom;
 
@@ -882,7 +988,7 @@ k_finalize(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms
     vec3 pi = xyz(p[i]);
     vec3 np = pi;
     vec3 rv = (np - xi) / dt;
-    const float rl = length(rv);
+    const float rl = length_exact(rv);
     if (rl > D.max_speed) {
         rv = (rv / rl) * D.max_speed;
         np = xi + rv * dt;
@@ -955,52 +1061,6 @@ k_grid_normals(const Tile* __restrict__ tiles, const DomainParams* __restrict__ 
     nrm[i] = make_float4(n.x, n.y, n.z, 0.0f);
 }
 
-// ------------------------------------------------------------------ device grid builder
-// VtClothObjectGPU::Start for a grid cloth (Velvet/VtClothObjectGPU.hpp:43-147) without
-// host loops: every particle evaluates its vertex, its inverse mass (0 when its distance
-// to a slot is 0, AddAttach's rule), its LRA rests |slot - x0_i| and, as generator (a, b),
-// the rest lengths of its four stretch constraints from the neighbouring vertices — the
-// values grid_rests reads from the host-built constraint list, by the same operations.
-__global__ void __launch_bounds__(kBlock)
-k_grid_build(float4* __restrict__ x, float4* __restrict__ v, float4* __restrict__ x0,
-             float4* __restrict__ grest, float4* __restrict__ glra, GridBuildArgs g)
-{
-    const int V = g.res + 1;
-    const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-    if (i >= (int64_t)V * V) return;
-    const int a = (int)(i / V), b = (int)(i - (int64_t)a * V), R = g.res;
-    const vec3 p = grid_vertex(a, b, R, g.size, g.model);
-    float w = 1.0f;
-    float r[kGridLraCached] = {0, 0, 0, 0};
-#pragma unroll
-    for (int s = 0; s < kGridLraCached; ++s)
-        if (s < g.ns) {
-            const float dist = length(xyz(g.slot[s]) - p);
-            if (dist == 0) w = 0;
-            r[s] = dist;
-        }
-    float4 gr = make_float4(0, 0, 0, 0);
-    if (b < R) gr.x = length(p - grid_vertex(a, b + 1, R, g.size, g.model));
-    if (a < R) gr.y = length(p - grid_vertex(a + 1, b, R, g.size, g.model));
-    if (a < R && b < R) {
-        gr.z = length(p - grid_vertex(a + 1, b + 1, R, g.size, g.model));
-        gr.w = length(grid_vertex(a, b + 1, R, g.size, g.model) - grid_vertex(a + 1, b, R, g.size, g.model));
-    }
-    x[i] = make_float4(p.x, p.y, p.z, w);
-    x0[i] = make_float4(p.x, p.y, p.z, 0.0f);
-    v[i] = make_float4(0, 0, 0, 0);
-    grest[i] = gr;
-    glra[i] = make_float4(r[0], r[1], r[2], r[3]);
-}
-
-cudaError_t launch_grid_build(const DeviceArrays& d, int64_t pb, const GridBuildArgs& g, cudaStream_t st)
-{
-    const int64_t n = (int64_t)(g.res + 1) * (g.res + 1);
-    k_grid_build<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, st>>>(d.x + pb, d.v + pb, d.x0 + pb,
-                                                                         d.grest + pb, d.glra + pb, g);
-    return cudaGetLastError();
-}
-
 // ------------------------------------------------------------------ read-back packing
 __global__ void __launch_bounds__(kBlock) k_pack_xyz(const float4* __restrict__ src, float* __restrict__ dst,
                                                       int64_t n)
@@ -1033,7 +1093,8 @@ cudaError_t launch_collide(const Launch& L, int pin, int pout)
 {
     if (!L.n_ptiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
-    k_collide<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.col, d.x, d.p[pin], d.p[pout], d.nbr, d.status);
+    k_collide<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.col, d.x, d.p[pin], d.p[pout], d.nbr, d.vals,
+                                               d.dslot, d.status);
     return cudaGetLastError();
 }
 
@@ -1100,8 +1161,9 @@ static void grid_iter_variant(const Launch& L, int pin, int pout, int mode)
 {
     constexpr GridVariant g = kGridVariant[v];
     const DeviceArrays& d = *L.d;
+    const CUtensorMap* tm = tile_loads_tma() ? d.tmaps : nullptr;
 #define VT_GRID_ARGS \
-    d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.grest, d.glra, d.slots, d.slots0, d.status
+    d.gtiles, d.dom, d.p[pin], d.p[pout], d.x, d.v, d.x0, d.grest, d.glra, d.slots, d.slots0, d.status, tm, pin
     if (mode == SOLVE_PLAIN)
         k_grid_iter<SOLVE_PLAIN, g.ta, g.tb, g.blocks><<<L.n_gtiles, kBlock, 0, L.st>>>(VT_GRID_ARGS);
     else if (mode == SOLVE_FINALIZE)

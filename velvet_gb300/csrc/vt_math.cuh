@@ -5,9 +5,13 @@
 //   normalize(v)   = v * (1 / sqrt(dot(v, v)))
 //   mat4 * vec4    = (c0*x + c1*y) + (c2*z + c3*w)
 //   mat3 * vec3    = (c0*x + c1*y) + c2*z
-// The translation units that include this file are compiled with -fmad=false, so no
-// multiply-add pair is contracted into an FMA: every result is the IEEE-rounded value
-// of the operations as written, on the device and in host code alike.
+// The exact build compiles the translation units that include this file with
+// -fmad=false, so no multiply-add pair is contracted into an FMA: every result is the
+// IEEE-rounded value of the operations as written, on the device and in host code alike.
+// The fast build (VT_FAST, device code only) divides a vector by one reciprocal, takes
+// normalize's reciprocal square root in one step and calls CUDA's acosf; with its
+// compiler flags (contraction, approximate division and square root) its results are
+// within the solver's stated tolerance of the exact ones, not equal to them.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -15,6 +19,12 @@
 
 #define VT_HD __host__ __device__ __forceinline__
 #define VT_EPSILON 1e-6f  // EPSILON, Velvet/Common.cuh:12
+
+#if defined(VT_FAST) && defined(__CUDA_ARCH__)
+#define VT_FAST_DEVICE 1
+#else
+#define VT_FAST_DEVICE 0
+#endif
 
 struct vec3 {
     float x, y, z;
@@ -26,14 +36,84 @@ VT_HD vec3 operator+(vec3 a, vec3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.
 VT_HD vec3 operator-(vec3 a, vec3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
 VT_HD vec3 operator-(vec3 a) { return mk3(-a.x, -a.y, -a.z); }
 VT_HD vec3 operator*(vec3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
-VT_HD vec3 operator/(vec3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+VT_HD vec3 operator/(vec3 a, float s)
+{
+#if VT_FAST_DEVICE
+    const float r = 1.0f / s;
+    return mk3(a.x * r, a.y * r, a.z * r);
+#else
+    return mk3(a.x / s, a.y / s, a.z / s);
+#endif
+}
 VT_HD vec3 cmul(vec3 a, vec3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
 VT_HD float dot(vec3 a, vec3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 VT_HD float length(vec3 a) { return sqrtf(dot(a, a)); }
-VT_HD vec3 normalize(vec3 a) { return a * (1.0f / sqrtf(dot(a, a))); }
+VT_HD vec3 normalize(vec3 a)
+{
+#if VT_FAST_DEVICE
+    return a * rsqrtf(dot(a, a));
+#else
+    return a * (1.0f / sqrtf(dot(a, a)));
+#endif
+}
+// The squared distance and distance a threshold decision is taken on (a stretch
+// constraint at its rest length, an attachment beyond its target, a contact closer than
+// the particle diameter, a particle inside a sphere).  Such a decision changes the count
+// the Jacobi update is averaged over, so the fast build takes these values with the exact
+// build's operations — IEEE products, sums and square root, no contraction — and fires a
+// constraint exactly when the exact build does on the same positions; only the
+// corrections themselves use the fast arithmetic.
+VT_HD float dot_exact(vec3 a, vec3 b)
+{
+#if VT_FAST_DEVICE
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+#else
+    return dot(a, b);
+#endif
+}
+VT_HD float sqrt_exact(float q)
+{
+#if VT_FAST_DEVICE
+    return __fsqrt_rn(q);
+#else
+    return sqrtf(q);
+#endif
+}
+VT_HD float length_exact(vec3 a) { return sqrt_exact(dot_exact(a, a)); }
 VT_HD vec3 cross(vec3 a, vec3 b)
 {
     return mk3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+// The dihedral angle of a bending constraint is acos of a dot product of unit normals;
+// for a nearly flat pair the dot is within a few ulps of 1, where acos magnifies each ulp
+// of it ~1e4-fold.  The fast build therefore takes the whole chain — the two normals, their
+// scaling and normalisation, the dot, acos and the sign test — with the exact build's
+// operations, so the angle has the exact build's bits on the same positions.
+VT_HD vec3 cross_exact(vec3 a, vec3 b)
+{
+#if VT_FAST_DEVICE
+    return mk3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(b.y, a.z)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(b.z, a.x)),
+               __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(b.x, a.y)));
+#else
+    return cross(a, b);
+#endif
+}
+VT_HD vec3 div_exact(vec3 a, float s)
+{
+#if VT_FAST_DEVICE
+    return mk3(__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s));
+#else
+    return mk3(a.x / s, a.y / s, a.z / s);
+#endif
+}
+VT_HD vec3 normalize_exact(vec3 a)
+{
+#if VT_FAST_DEVICE
+    const float r = __fdiv_rn(1.0f, __fsqrt_rn(dot_exact(a, a)));
+    return mk3(__fmul_rn(a.x, r), __fmul_rn(a.y, r), __fmul_rn(a.z, r));
+#else
+    return a * (1.0f / sqrtf(dot(a, a)));
+#endif
 }
 // glm::clamp: min(max(x, lo), hi) with glm's ternary min / max (NaN passes through)
 VT_HD float gclamp(float x, float lo, float hi)
@@ -106,6 +186,9 @@ VT_HD float vt_asin_series(float t)
 
 VT_HD float vt_acosf(float x)
 {
+#if VT_FAST_DEVICE
+    return acosf(x);
+#else
     const float pio2_hi = 1.57079637050628662109375f;
     const float pio2_lo = -4.37113900018624283e-8f;
     if (x >= 0.5f) {
@@ -117,6 +200,34 @@ VT_HD float vt_acosf(float x)
         return ((pio2_hi - vt_asin_series(s)) + pio2_lo) * 2.0f;
     }
     return (pio2_hi - vt_asin_series(x)) + pio2_lo;
+#endif
+}
+
+// vt_acosf with every operation rounded as written (the fast build's exact angle chain).
+VT_HD float vt_acosf_exact(float x)
+{
+#if VT_FAST_DEVICE
+    const float c[11] = {0.16666666666666666f, 0.075f, 0.044642857142857144f, 0.030381944444444444f,
+                         0.022372159090909092f, 0.017352764423076924f, 0.01396484375f, 0.011551800896139705f,
+                         0.009761609529194078f, 0.008390335809616815f, 0.0073125258735988454f};
+    auto series = [&](float t) {
+        const float z = __fmul_rn(t, t);
+        float p = c[10];
+#pragma unroll
+        for (int k = 9; k >= 0; --k) p = __fadd_rn(__fmul_rn(p, z), c[k]);
+        return __fadd_rn(t, __fmul_rn(t, __fmul_rn(z, p)));
+    };
+    const float pio2_hi = 1.57079637050628662109375f;
+    const float pio2_lo = -4.37113900018624283e-8f;
+    if (x >= 0.5f) return __fmul_rn(2.0f, series(__fsqrt_rn(__fmul_rn(__fsub_rn(1.0f, x), 0.5f))));
+    if (x <= -0.5f)
+        return __fmul_rn(__fadd_rn(__fsub_rn(pio2_hi, series(__fsqrt_rn(__fmul_rn(__fadd_rn(1.0f, x), 0.5f)))),
+                                   pio2_lo),
+                         2.0f);
+    return __fadd_rn(__fsub_rn(pio2_hi, series(x)), pio2_lo);
+#else
+    return vt_acosf(x);
+#endif
 }
 
 // Vertex (a, b) of GenerateClothMesh (Velvet/Scene.hpp:131-168) for a cloth of side

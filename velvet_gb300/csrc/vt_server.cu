@@ -165,6 +165,8 @@ struct vt_server {
     std::vector<vt::DomainParams> hdom;
     std::vector<vt::ColliderDev> hcol;
     std::vector<float4> hslots, hslots0;
+    CUtensorMap* tmaps = nullptr;          // device: kTmapsPerDomain per slot id
+    std::vector<CUtensorMap> htmaps;       // host copy, encoded at admission
     int32_t n_ptiles = 0, n_gtiles = 0, grid_variant = 0;
     std::vector<std::pair<double, int32_t>> frame_log;  // (frame ms, active requests)
     vt_server_stats stats{};
@@ -234,7 +236,7 @@ vt_status fill_slot_tables(vt_server* s, const Request* r)
     D.col_count = (int32_t)h.colliders.size();
     D.table_base = (int32_t)(3 * pb);
     D.table_size = h.table_size;
-    D.nbr_base = (int32_t)(kMaxNbr * pb);
+    vt::set_nbr_offset(D, (int64_t)kMaxNbr * pb);
     D.max_nbr = h.P.max_num_neighbors;
     D.cell_spacing = h.cell_spacing;
     D.cell_spacing2 = h.cell_spacing * h.cell_spacing;
@@ -244,6 +246,10 @@ vt_status fill_slot_tables(vt_server* s, const Request* r)
     D.grid_slot_count = h.grid_slot_count;
     vt::fill_frame_params(D, h.P, frame_args(s, h));
     s->hdom[sid] = D;
+    // the tile kernel's tensor maps for this request's range of the arena
+    if (!vt::encode_grid_tmaps(&s->htmaps[vt::tmap_index(sid, 0, 0)], s->d.p[0], s->d.p[1], s->d.grest, s->d.glra,
+                               s->d.x, (int64_t)pb, h.grid_res + 1))
+        return VT_ERR_CUDA;
     for (size_t k = 0; k < h.colliders.size(); ++k)
         s->hcol[sid * kCollidersPerCloth + k] = vt::collider_to_device(h.colliders[k]);
     for (int32_t k = 0; k < h.grid_slot_count; ++k) {
@@ -326,6 +332,11 @@ vt_status upload_tables(vt_server* s, cudaStream_t st)
         return e;
     };
     VT_TRY_CUDA(put(s->d.dom, s->hdom.data(), sizeof(vt::DomainParams) * s->hdom.size()), "upload params");
+    int32_t used = 0;  // slot ids below the highest active one
+    for (int32_t sid = 0; sid < (int32_t)s->slot.size(); ++sid)
+        if (s->slot[sid]) used = sid + 1;
+    VT_TRY_CUDA(put(s->tmaps, s->htmaps.data(), sizeof(CUtensorMap) * vt::kTmapsPerDomain * (size_t)used),
+                "upload tensor maps");
     VT_TRY_CUDA(put(s->d.col, s->hcol.data(), sizeof(vt::ColliderDev) * s->hcol.size()), "upload colliders");
     VT_TRY_CUDA(put(s->d.slots, s->hslots.data(), 16 * s->hslots.size()), "upload slots");
     VT_TRY_CUDA(put(s->d.slots0, s->hslots0.data(), 16 * s->hslots0.size()), "upload slots0");
@@ -410,7 +421,9 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
                                 2 * 16 * kSlotsPerCloth + 4) + (1 << 20);
     VT_CHECK(cfg->hbm_budget_bytes > fixed + 1024 * kBytesPerParticle, VT_ERR_CAPACITY, "budget too small");
     int64_t cap = (int64_t)((cfg->hbm_budget_bytes - fixed) / kBytesPerParticle);
-    cap = std::min<int64_t>(cap, (int64_t)INT32_MAX / kMaxNbr - 1);
+    // particle indices, sorted slots and cell keys (3 cells per arena particle) are 32-bit;
+    // neighbour-list offsets are 64-bit (nbr_offset)
+    cap = std::min<int64_t>(cap, ((int64_t)INT32_MAX - 16) / 3);
     // tile tables: sides up to sqrt(cap); generators per tile 217 particles
     const int64_t cap_pt = cap / 256 + M + 1;
     // grid tiles of the shape with the most tiles (3 x 63: ~V^2/189 + V/3 per cloth)
@@ -421,7 +434,8 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     const size_t hist = (vt::radix_hist_words((int32_t)cap) * 4 + 255) & ~size_t(255);
     const size_t cells = ((size_t)cap * 3 * 4 + 255) & ~size_t(255), nbr = (size_t)cap * kMaxNbr * 4;
     const size_t small = M * (sizeof(vt::DomainParams) + kCollidersPerCloth * sizeof(vt::ColliderDev) +
-                              2 * 16 * kSlotsPerCloth) + 4 * (M + 1) + 4096 * 4;
+                              2 * 16 * kSlotsPerCloth) + 4 * (M + 1) + 4 * M + 4096 * 4 +
+                         M * vt::kTmapsPerDomain * sizeof(CUtensorMap) + 256;
     const size_t a12 = ((size_t)cap * 12 + 255) & ~size_t(255);
     const size_t total = 10 * a16 + 5 * a4 + a12 + hist + 2 * cells + nbr + small +
                          tiles_bytes(cap_pt, sizeof(vt::Tile)) * 2 + tiles_bytes(cap_gt, sizeof(vt::GridTile)) +
@@ -445,6 +459,10 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     s->d.slots = (float4*)take(M * kSlotsPerCloth * 16);
     s->d.slots0 = (float4*)take(M * kSlotsPerCloth * 16);
     s->d.status = (int32_t*)take(4 * (M + 1));
+    s->d.dslot = (int32_t*)take(4 * M);
+    s->tmaps = (CUtensorMap*)take(M * vt::kTmapsPerDomain * sizeof(CUtensorMap));
+    s->d.tmaps = s->tmaps;
+    s->htmaps.assign(M * vt::kTmapsPerDomain, CUtensorMap{});
     s->d.ptiles = (vt::Tile*)take(cap_pt * sizeof(vt::Tile));
     s->d.gptiles = (vt::Tile*)take(cap_pt * sizeof(vt::Tile));
     s->d.gtiles = (vt::GridTile*)take(cap_gt * sizeof(vt::GridTile));
@@ -456,7 +474,7 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     VT_TRY_CUDA(cudaMemset(s->d.status, 0, 4 * (M + 1)), "init status");
     VT_TRY_CUDA(cudaMemset(s->d.nbr, 0xff, nbr), "init neighbours");
     s->staging_bytes = M * (sizeof(vt::DomainParams) + kCollidersPerCloth * sizeof(vt::ColliderDev) +
-                            2 * 16 * kSlotsPerCloth) +
+                            2 * 16 * kSlotsPerCloth + vt::kTmapsPerDomain * sizeof(CUtensorMap)) +
                       cap_pt * 2 * sizeof(vt::Tile) + cap_gt * sizeof(vt::GridTile) + 16 * 256;
     VT_TRY_CUDA(cudaMallocHost(&s->staging, s->staging_bytes), "cudaMallocHost(server staging)");
     VT_TRY_CUDA(cudaEventCreateWithFlags(&s->staged, cudaEventDisableTiming), "event");
@@ -712,6 +730,10 @@ vt_status vt_server_tick(vt_server* s, void* stream, vt_server_tick_info* info)
         if (s->status_pin[prev][0] & vt::VT_STATUS_BOUNDS) {
             vt::set_error("a device-side bounds check failed (bounds-checked build)");
             return VT_ERR_STATE;
+        }
+        if (s->status_pin[prev][0] & vt::VT_STATUS_TIMEOUT) {
+            vt::set_error("a device-side bounded wait gave up (tile loads did not arrive)");
+            return VT_ERR_TIMEOUT;
         }
         for (const auto& m : s->members[prev]) {
             m.first->done += 1;

@@ -14,9 +14,13 @@
 //       grid_iter (grid domains) and bend + solve (CSR domains); the last iteration
 //       also runs Finalize and, except after the last substep, the next Predict
 //   normals
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
+#include <string>
 
 #include "vt_host.h"
 #include "vt_math.cuh"
@@ -185,6 +189,73 @@ int last_tuned_variant()
 {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     return g_forced_variant >= 0 ? g_forced_variant : g_last_tuned;
+}
+
+// ------------------------------------------------------------------ tensor maps
+namespace {
+std::atomic<bool> g_tile_tma{true};
+
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// A V x V grid of float4 at base as a 3-D FP32 tensor (xyzw, column, row) with a box of
+// bw columns by bh rows.
+bool encode_one(CUtensorMap* m, const float4* base, int V, int bw, int bh)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return false;
+    }
+    const cuuint64_t dims[3] = {4, (cuuint64_t)V, (cuuint64_t)V};
+    const cuuint64_t strides[2] = {16, (cuuint64_t)V * 16};  // bytes, dims 1 and 2
+    const cuuint32_t box[3] = {4, (cuuint32_t)bw, (cuuint32_t)bh};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float4*>(base), dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        return false;
+    }
+    return true;
+}
+}  // namespace
+
+bool encode_grid_tmaps(CUtensorMap* dst, const float4* p0, const float4* p1, const float4* grest,
+                       const float4* glra, const float4* x, int64_t p_begin, int V)
+{
+    static_assert(sizeof(CUtensorMap) == 128, "tensor map size");
+    const int shapes[kTmapShapes][2] = {{7, 31}, {15, 15}, {3, 63}};
+    for (int sh = 0; sh < kTmapShapes; ++sh) {
+        const int ta = shapes[sh][0], tb = shapes[sh][1];
+        CUtensorMap* m = dst + tmap_index(0, sh, 0);
+        if (!encode_one(m + TMAP_P0, p0 + p_begin, V, tb + 2, ta + 2) ||
+            !encode_one(m + TMAP_P1, p1 + p_begin, V, tb + 2, ta + 2) ||
+            !encode_one(m + TMAP_GREST, grest + p_begin, V, tb + 1, ta + 1) ||
+            !encode_one(m + TMAP_GLRA, glra + p_begin, V, tb, ta) || !encode_one(m + TMAP_X, x + p_begin, V, tb, ta))
+            return false;
+    }
+    return true;
+}
+
+bool tile_loads_tma() { return g_tile_tma.load(); }
+vt_status set_tile_loads_tma(bool on)
+{
+    g_tile_tma.store(on);
+    return VT_OK;
 }
 
 vt_status tuning_force(int32_t variant)
@@ -530,7 +601,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         D.col_count = (int32_t)h.colliders.size();
         D.table_base = tkb;
         D.table_size = h.table_size;
-        D.nbr_base = nwb;
+        vt::set_nbr_offset(D, nwb);
         D.max_nbr = h.P.max_num_neighbors;
         D.cell_spacing = h.cell_spacing;
         D.cell_spacing2 = h.cell_spacing * h.cell_spacing;
@@ -596,6 +667,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_grest = A.take<float4>(any_grid ? N : 0), o_glra = A.take<float4>(any_grid ? N : 0);
     const size_t o_st = A.take<int32_t>(1 + n_domains), o_pk = A.take<float>(3 * (size_t)N);
     const size_t o_ps = A.take<float4>(N), o_x0s = A.take<float4>(N);
+    const size_t o_tm = A.take<CUtensorMap>(any_grid ? (size_t)kTmapsPerDomain * n_domains : 0);
     bytes = A.off;
     VT_CUDA(cudaMalloc(&arena_, A.off), "cudaMalloc(world)");
     char* base = (char*)arena_;
@@ -617,6 +689,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     d.stiles = AT(Tile, o_stt); d.gtiles = AT(GridTile, o_gt); d.gptiles = AT(Tile, o_gpt);
     d.grest = AT(float4, o_grest); d.glra = AT(float4, o_glra); d.packed = AT(float, o_pk);
     d.ps = AT(float4, o_ps); d.x0s = AT(float4, o_x0s);
+    CUtensorMap* tmaps_dev = any_grid ? AT(CUtensorMap, o_tm) : nullptr;
 #undef AT
     auto up = [](void* dst, const void* src, size_t bytes_) -> cudaError_t {
         return bytes_ ? cudaMemcpy(dst, src, bytes_, cudaMemcpyHostToDevice) : cudaSuccess;
@@ -652,6 +725,17 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     if (any_grid) {
         VT_CUDA(up(d.grest, hgrest.data(), N * 16), "upload grest");
         VT_CUDA(up(d.glra, hglra.data(), N * 16), "upload glra");
+        // the tile kernel's tensor maps (zeroed for domains the CSR kernels solve)
+        std::vector<CUtensorMap> htm((size_t)kTmapsPerDomain * n_domains);
+        std::memset(htm.data(), 0, htm.size() * sizeof(CUtensorMap));
+        for (auto& gd : grid_doms_) {
+            const DomainParams& D = hdom[gd.first];
+            if (!encode_grid_tmaps(htm.data() + tmap_index(gd.first, 0, 0), d.p[0], d.p[1], d.grest, d.glra, d.x,
+                                   D.p_begin, D.grid_res + 1))
+                return VT_ERR_CUDA;
+        }
+        VT_CUDA(up(tmaps_dev, htm.data(), htm.size() * sizeof(CUtensorMap)), "upload tensor maps");
+        d.tmaps = tmaps_dev;
     }
     VT_CUDA(prepare_kernels(), "kernel attributes");
     tuned_ = false;

@@ -21,11 +21,15 @@
 //               corner slots per particle in constraint order
 //   normals     tn_off/tn_ent CSR of triangles per vertex; tri uint4 per triangle
 //   hash        keys/vals (sorted pairs), cell_start (sum of (T_d + 1)), cell_end,
-//               neighbours (max_nbr * n_d per domain, column-major inside a domain)
+//               neighbours (max_nbr * n_d per domain, column-major inside a domain, in
+//               sorted-slot order: the list of the particle in the domain's r-th sorted
+//               slot is column r, so the walk that writes the lists and the collision
+//               pass that reads them both run in sorted order and access whole rows)
 #pragma once
 
 #include <cstdint>
 #include <vector>
+#include <cuda.h>  // CUtensorMap (the type only; maps are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #include "../../include/velvet_gb300.h"
@@ -41,7 +45,7 @@ namespace vt {
 #ifndef VT_CHECKED
 #define VT_CHECKED 0
 #endif
-constexpr int32_t VT_STATUS_NONFINITE = 1, VT_STATUS_BOUNDS = 2;
+constexpr int32_t VT_STATUS_NONFINITE = 1, VT_STATUS_BOUNDS = 2, VT_STATUS_TIMEOUT = 4;
 #if VT_CHECKED
 __device__ __forceinline__ bool vt_in_range(long long v, long long lo, long long hi, int32_t* status)
 {
@@ -59,7 +63,8 @@ struct DomainParams {
     int32_t p_begin, p_count;      // particle range
     int32_t col_begin, col_count;  // colliders
     int32_t table_base, table_size; // hash cells [table_base, table_base + table_size)
-    int32_t nbr_base, max_nbr;     // neighbour block of this domain
+    uint32_t nbr_base_lo;          // neighbour block of this domain (low 32 bits; nbr_offset)
+    int32_t max_nbr;
     float cell_spacing, cell_spacing2, diameter, diameter2;
     float gx, gy, gz;
     float dt_frame, dt_sub;
@@ -69,9 +74,22 @@ struct DomainParams {
     int32_t grid_slot_begin, grid_slot_count;  // its LRA slots (global slot indices)
     float xpbd_bend;         // bend_compliance / dt_sub / dt_sub, evaluated in that order
     uint32_t tmod_lo, tmod_hi;  // floor((2^64 - 1) / table_size) + 1, for the cell-key remainder
-    int32_t pad_;               // 128 bytes: kernels stage the block in 16-byte copies
+    uint32_t nbr_base_hi;       // high 32 bits of the neighbour block offset (128 bytes:
+                                // kernels stage the block in 16-byte copies)
 };
 static_assert(sizeof(DomainParams) == 128, "DomainParams layout");
+
+// Offset of a domain's neighbour block in 32-bit words: 64-bit, since the served form's
+// arena can hold more than 2^31 list words (64 per particle).
+__host__ __device__ __forceinline__ int64_t nbr_offset(const DomainParams& D)
+{
+    return (int64_t)(((uint64_t)D.nbr_base_hi << 32) | (uint64_t)D.nbr_base_lo);
+}
+inline void set_nbr_offset(DomainParams& D, int64_t words)
+{
+    D.nbr_base_lo = (uint32_t)(uint64_t)words;
+    D.nbr_base_hi = (uint32_t)((uint64_t)words >> 32);
+}
 
 // The 64-bit reciprocal of a hash table size used by the direct-remainder modulo.
 inline void set_table_magic(DomainParams& D)
@@ -112,6 +130,29 @@ inline void grid_tiles_for(std::vector<GridTile>& out, int dom, const DomainPara
         for (int b = 0; b < V; b += g.tb)
             out.push_back(GridTile{dom, a, b, D.grid_res, D.p_begin, D.grid_slot_begin, D.grid_slot_count, 0});
 }
+
+// Tensor maps for the tile kernel's TMA loads.  Per grid domain and tile shape (7x31,
+// 15x15, 3x63: the variants' shapes in order), one 3-D map (float xyzw, column b, row a)
+// of each array the kernel stages: the two predicted-position buffers, the generators'
+// rest lengths, the particles' LRA rests and positions, with the box of that shape
+// (halo tile, generator tile, particle tile).  Out-of-range boxes are filled with zeros,
+// as the cp.async path's zero-fill does.
+constexpr int kTmapShapes = 3;
+constexpr int kTmapKinds = 5;  // p[0], p[1], grest, glra, x
+constexpr int kTmapsPerDomain = kTmapShapes * kTmapKinds;
+enum TmapKind { TMAP_P0 = 0, TMAP_P1 = 1, TMAP_GREST = 2, TMAP_GLRA = 3, TMAP_X = 4 };
+__host__ __device__ constexpr int tmap_shape_of(int ta) { return ta == 7 ? 0 : (ta == 15 ? 1 : 2); }
+__host__ __device__ constexpr int tmap_index(int dom, int shape, int kind)
+{
+    return (dom * kTmapShapes + shape) * kTmapKinds + kind;
+}
+// Encodes the kTmapsPerDomain maps of the V x V grid cloth whose first particle is p_begin
+// into dst.  Returns false (with the error set) if the driver refuses a map.
+bool encode_grid_tmaps(CUtensorMap* dst, const float4* p0, const float4* p1, const float4* grest,
+                       const float4* glra, const float4* x, int64_t p_begin, int V);
+// Whether the tile kernel stages its tiles with TMA (default) or per-thread cp.async.
+bool tile_loads_tma();
+vt_status set_tile_loads_tma(bool on);
 
 // One collider on the device: the reference's SDFCollider with VelocityAt's matrix
 // product lastTransform * invCurTransform precomputed (same arithmetic, once per frame).
@@ -168,6 +209,13 @@ struct DeviceArrays {
     float* packed = nullptr;    // 3 floats per particle: read-back staging (contiguous xyz)
     // predicted and initial positions in sorted-slot order, rebuilt with every hash
     float4 *ps = nullptr, *x0s = nullptr;
+    // tensor maps of the grid domains' arrays for the tile kernel's TMA loads:
+    // kTmapsPerDomain per domain (tmap_index); nullptr: the kernel stages with cp.async
+    const CUtensorMap* tmaps = nullptr;
+    // served form only: the first sorted slot of each domain, rebuilt with every hash (a
+    // domain's particles fill consecutive sorted slots; with free arena ranges between
+    // requests they do not start at p_begin).  nullptr elsewhere: slots = particle range.
+    int32_t* dslot = nullptr;
 };
 
 // ------------------------------------------------------------------ kernel launchers
