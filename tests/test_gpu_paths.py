@@ -120,7 +120,7 @@ def test_every_grid_tile_shape_gives_the_same_bits(variant, side):
 @pytest.mark.parametrize("variant", [0, 2, 4])
 def test_tile_loads_by_tma_and_by_cp_async_give_the_oracle_bits(variant, tma):
     """The tile kernel stages its halo, rests and positions with TMA bulk tensor copies
-    (default) or per-thread cp.async (vt_tuning_set_tile_loads): both give the oracle's
+    or per-thread cp.async (the default; vt_tuning_set_tile_loads): both give the oracle's
     bits, for every tile shape, on a cloth with partial tiles, two cached LRA slots and
     the finalizing iterations' position loads, and on a batch of cloths of several sizes."""
     assert vg.lib().vt_tuning_set_tile_loads(tma) == 0
@@ -153,7 +153,7 @@ def test_tile_loads_by_tma_and_by_cp_async_give_the_oracle_bits(variant, tma):
             same(batch.positions(k), a.positions(), f"tile loads {tma}, batch cloth {k}")
     finally:
         vg.lib().vt_tuning_set_grid_tile(-1)
-        vg.lib().vt_tuning_set_tile_loads(1)
+        vg.lib().vt_tuning_set_tile_loads(0)
 
 
 @pytest.mark.parametrize("variant", [-1, 1, 5])

@@ -890,9 +890,8 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     const bool tma = tmaps != nullptr;
     const bool stage_lra = ns >= 1 && ns <= kGridLraCached;
     if (tma) {
-        if (tid == 0) mbar_init(&sbar, 1);
-        __syncthreads();  // the barrier is initialised before anyone waits on it
-        if (tid == 0) {
+        if (tid == 0) {  // the barrier is published to the block by the __syncthreads below
+            mbar_init(&sbar, 1);
             const CUtensorMap* m = tmaps + tmap_index(tl.dom, tmap_shape_of(kTA), 0);
             const uint32_t bytes = 16u * (uint32_t)(kGHA * kGHB + kGGA * kGGB + (stage_lra ? kTA * kTB : 0) +
                                                    (kMode != SOLVE_PLAIN ? kTA * kTB : 0));
@@ -921,15 +920,15 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     if (tid < (int)(sizeof(DomainParams) / 16))
         cp_async16(reinterpret_cast<float4*>(&sdom) + tid, reinterpret_cast<const float4*>(doms + tl.dom) + tid);
     cp_async_wait_all();
-    if (tma) {
-        // every thread waits for the copies; if any gave up, the block reports it and ends
-        const bool arrived = mbar_wait(&sbar, 0);
-        if (__syncthreads_or(!arrived)) {
-            if (tid == 0) atomicOr(status, VT_STATUS_TIMEOUT);
-            return;
-        }
+    __syncthreads();
+    if (tma && !mbar_wait(&sbar, 0)) {
+        // the copies did not arrive in time: report it (the sync calls return
+        // VT_ERR_TIMEOUT) and finish the block on whatever the tile holds, without a
+        // barrier that the other threads might not reach
+        atomicOr(status, VT_STATUS_TIMEOUT);
+    }
 #if VT_CHECKED
-        // the bounds-checked build compares the staged halo with the global array
+    if (tma) {  // the bounds-checked build compares the staged halo with the global array
         for (int k = tid; k < kGHA * kGHB; k += kBlock) {
             const int ha = k / kGHB, hb = k - ha * kGHB;
             const int pa = a0 - 1 + ha, pb = b0 - 1 + hb;
@@ -940,9 +939,8 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
                 __float_as_uint(got.z) != __float_as_uint(want.z) || __float_as_uint(got.w) != __float_as_uint(want.w))
                 atomicOr(status, VT_STATUS_BOUNDS);
         }
-#endif
     }
-    __syncthreads();
+#endif
     const DomainParams& D = sdom;
 
     // 2. the slot groups' boxes when the cloth has more LRA slots than the cache holds

@@ -193,7 +193,7 @@ int last_tuned_variant()
 
 // ------------------------------------------------------------------ tensor maps
 namespace {
-std::atomic<bool> g_tile_tma{true};
+std::atomic<bool> g_tile_tma{false};  // per-thread cp.async measured faster (see vt_tuning_set_tile_loads)
 
 PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
 {

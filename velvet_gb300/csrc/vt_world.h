@@ -150,7 +150,7 @@ __host__ __device__ constexpr int tmap_index(int dom, int shape, int kind)
 // into dst.  Returns false (with the error set) if the driver refuses a map.
 bool encode_grid_tmaps(CUtensorMap* dst, const float4* p0, const float4* p1, const float4* grest,
                        const float4* glra, const float4* x, int64_t p_begin, int V);
-// Whether the tile kernel stages its tiles with TMA (default) or per-thread cp.async.
+// Whether the tile kernel stages its tiles with TMA or with per-thread cp.async (default).
 bool tile_loads_tma();
 vt_status set_tile_loads_tma(bool on);
 
