@@ -65,6 +65,13 @@ def workload(name: str, seed: int = 0):
         return W.batched(512, seed=seed)
     if name == "small":
         return W.small()
+    if name == "small32":  # the small configuration's setting on a 32x32 cloth
+        wl = W.small()
+        spec = wl.cloths[0]
+        wl.cloths[0] = W.ClothSpec(32, spec.spacing, W.horizontal_cloth(32, spec.spacing, 0.8), [0, 31],
+                                   spec.colliders)
+        wl.name = "small_32x32"
+        return wl
     if name == "large":
         return W.large()
     if name == "stress":
@@ -730,6 +737,8 @@ def main() -> None:
     ap.add_argument("--no-served", action="store_true", help="skip the served leg")
     ap.add_argument("--tile-loads", choices=["tma", "cp_async"], default="cp_async",
                     help="how the grid kernel stages its tiles (same results)")
+    ap.add_argument("--substep-clusters", choices=["on", "off"], default="on",
+                    help="small grid cloths: a substep's iterations as one launch of thread-block clusters")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs")
     ap.add_argument("--no-exact-build", action="store_true",
                     help="skip timing the exact build beside the fast one")
@@ -749,6 +758,10 @@ def main() -> None:
         import velvet_gb300 as vg
 
         vg._abi.check(vg.lib().vt_tuning_set_tile_loads(1), "vt_tuning_set_tile_loads")
+    if args.substep_clusters == "off":
+        import velvet_gb300 as vg
+
+        vg._abi.check(vg.lib().vt_tuning_set_substep_clusters(0), "vt_tuning_set_substep_clusters")
     if args.profile_frames:
         profile_frames(args)
         return
@@ -990,7 +1003,7 @@ def main() -> None:
             "data": "synthetic grid cloths generated from the config (seeded), no dataset",
             "config": {"workload": wl.name, "form": "batched (one graph launch per frame for all cloths)",
                        "library": f"libvelvet_gb300{'_fast' if args.variant == 'fast' else ''}.so",
-                       "tile_loads": args.tile_loads,
+                       "tile_loads": args.tile_loads, "substep_clusters": args.substep_clusters,
                        "cloths_per_gpu": len(wl.cloths), "particles_per_gpu": n_tot,
                        "substeps": wl.substeps, "iterations": wl.iterations,
                        "grid_tile": None if CSR_KERNELS else grid_tile,

@@ -156,6 +156,72 @@ def test_tile_loads_by_tma_and_by_cp_async_give_the_oracle_bits(variant, tma):
         vg.lib().vt_tuning_set_tile_loads(0)
 
 
+@pytest.mark.parametrize("clusters", [1, 0], ids=["clusters", "per_iteration"])
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_substeps_in_clusters_give_the_oracle_bits(variant, clusters):
+    """Small grid cloths run a substep's iterations as one launch of 16-block clusters,
+    one per cloth, with the cluster barrier between iterations (or one launch per
+    iteration): the oracle's bits either way — a 40x40 cloth (9 to 14 tiles, one per block,
+    for the three shapes), a 24x24 one (fewer tiles than blocks), odd and even iteration counts,
+    the finalizing iterations between substeps, and a batch of small cloths."""
+    assert vg.lib().vt_tuning_set_substep_clusters(clusters) == 0
+    assert vg.lib().vt_tuning_set_grid_tile(variant) == 0
+    try:
+        for side, its in ((40, 10), (24, 3)):
+            spec = spec_of(side, 0.45)
+            o, g = Oracle(), vg.ClothSolver()
+            for s in (o, g):
+                W.build_plain(spec, s)
+            run_frames([o, g], spec, 3, substeps=3, iterations=its)
+            same(g.positions(), o.positions(), f"clusters {clusters}, shape {variant}, side {side}")
+            same(g.velocities(), o.velocities(), f"clusters {clusters}, shape {variant}, side {side} velocities")
+        wl = W.batched(6, frames=2, seed=4, lo=8, hi=44)
+        batch, alone = vg.BatchSolver(), []
+        for c in wl.cloths:
+            s = vg.ClothSolver()
+            W.build_plain(c, s)
+            batch.add(s)
+            s.close()
+            a = Oracle()
+            W.build_plain(c, a)
+            alone.append(a)
+        for f in range(wl.frames):
+            batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction, wl.collision_margin)
+            for a, c in zip(alone, wl.cloths):
+                a.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                           wl.collision_margin, c.particle_diameter())
+        batch.sync()
+        for k, a in enumerate(alone):
+            same(batch.positions(k), a.positions(), f"clusters {clusters}, batch cloth {k}")
+    finally:
+        vg.lib().vt_tuning_set_grid_tile(-1)
+        vg.lib().vt_tuning_set_substep_clusters(1)
+
+
+def test_substeps_in_clusters_cut_the_launches_of_a_small_cloth():
+    """With clusters, a 32x32 cloth's frame launches one grid kernel per substep instead of
+    one per iteration."""
+    import ctypes as C
+
+    counts = {}
+    for clusters in (1, 0):
+        assert vg.lib().vt_tuning_set_substep_clusters(clusters) == 0
+        try:
+            spec = spec_of(32, 0.45)
+            g = vg.ClothSolver()
+            W.build_plain(spec, g)
+            run_frames([g], spec, 3, substeps=5, iterations=10)  # past the autotuner's frame
+            n0 = C.c_uint64()
+            assert vg.lib().vt_solver_launch_count(g.handle, C.byref(n0)) == 0
+            run_frames([g], spec, 1, substeps=5, iterations=10)
+            n1 = C.c_uint64()
+            assert vg.lib().vt_solver_launch_count(g.handle, C.byref(n1)) == 0
+            counts[clusters] = n1.value - n0.value
+        finally:
+            vg.lib().vt_tuning_set_substep_clusters(1)
+    assert counts[0] - counts[1] == 5 * (10 - 1), counts
+
+
 @pytest.mark.parametrize("variant", [-1, 1, 5])
 @pytest.mark.parametrize("n_slots", [5, 24])
 def test_many_lra_slots_recompute_their_rests(n_slots, variant):

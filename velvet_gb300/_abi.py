@@ -223,6 +223,7 @@ SIGNATURES: dict[str, tuple] = {
     "vt_server_stats_get": (I32, [P, C.POINTER(VtServerStats)]),
     "vt_tuning_set_grid_tile": (I32, [I32]),
     "vt_tuning_set_tile_loads": (I32, [I32]),
+    "vt_tuning_set_substep_clusters": (I32, [I32]),
     "vt_solver_grid_tile": (I32, [P, PI32]),
     "vt_batch_grid_tile": (I32, [P, PI32]),
     "vt_camera_look_at": (I32, [PF, PF, PF, PF]),

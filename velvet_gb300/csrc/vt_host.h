@@ -160,6 +160,11 @@ private:
     int64_t frames_ = 0;  // frames simulated since the last build
     std::vector<std::pair<int32_t, int32_t>> grid_doms_;  // (domain, resolution) of grid domains
     int32_t gtiles_cap_ = 0;
+    // cluster-resident substeps (small grid cloths): per grid cloth its tile range
+    int2* cloth_tiles_dev_ = nullptr;
+    int32_t n_cluster_cloths_ = 0;
+    bool cluster_ok_ = false;
+    vt_status update_cluster_plan();
     // frame graph
     cudaStream_t cap_ = nullptr;
     cudaGraphExec_t gexec_ = nullptr;

@@ -845,33 +845,54 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
 // generators touching the tile once (one per thread: one bend + four stretch
 // constraints), then each particle sums its results in constraint order — the order of
 // the CSR kernel and of the oracle.
-template <int kMode, int kTA, int kTB, int kMinBlocks>
-__global__ void __launch_bounds__(kBlock, kMinBlocks)
-k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__ doms,
-            const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ x,
-            float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ grest,
-            const float4* __restrict__ glra, const float4* __restrict__ slots,
-            const float4* __restrict__ slots0, int32_t* __restrict__ status,
-            const CUtensorMap* __restrict__ tmaps, int pin_sel)
+// The shared memory of one tile (TMA destinations 128-byte aligned); kX = 0 leaves out the
+// positions the finalizing modes stage (plain iterations do not use them, and the
+// smaller footprint lets five blocks share an SM).
+template <int kTA, int kTB, int kX = 1>
+struct GridSmem {
+    static constexpr int kGHA = kTA + 2, kGHB = kTB + 2;  // halo tile
+    static constexpr int kGGA = kTA + 1, kGGB = kTB + 1;  // generators, kGGA * kGGB == kBlock
+    __align__(128) float4 sp[kGHA][kGHB];
+    __align__(128) float4 sst[4][kGGA][kGGB];  // stretch common + fired flag, per type
+    float4 sbd[4][kGGA][kGGB];                 // bending corner corrections + fired flag
+    __align__(128) float4 sgl[kBlock];         // the particle's LRA rest distances, or the slot groups' boxes
+    __align__(128) float4 sx[kX ? kBlock : 1];  // the particle's position (finalizing modes)
+    __align__(16) DomainParams sdom;
+    float4 sslot[kGridLraCached];
+    float4 ssup[4 * (kLraGroupsMax / kLraSuper)];  // the slot super-groups' boxes
+    uint64_t sbar;                                 // TMA completion barrier
+};
+
+// One tile's iteration, the body of k_grid_iter (and of each tile step of the cluster
+// kernel), on the block's shared tile `S`.  Threads may return before the end; a caller
+// that runs several tiles on one block separates them with __syncthreads.
+template <int kMode, int kTA, int kTB, int kX>
+__device__ __forceinline__ void grid_tile_iteration(GridSmem<kTA, kTB, kX>& S, const GridTile tl,
+                                                    const DomainParams* __restrict__ doms,
+                                                    const float4* __restrict__ pin, float4* __restrict__ pout,
+                                                    float4* __restrict__ x, float4* __restrict__ v,
+                                                    const float4* __restrict__ x0, const float4* __restrict__ grest,
+                                                    const float4* __restrict__ glra, const float4* __restrict__ slots,
+                                                    const float4* __restrict__ slots0, int32_t* __restrict__ status,
+                                                    const CUtensorMap* __restrict__ tmaps, int pin_sel)
 {
     constexpr int kGHA = kTA + 2, kGHB = kTB + 2;  // halo tile
     constexpr int kGGA = kTA + 1, kGGB = kTB + 1;  // generators, kGGA * kGGB == kBlock
     static_assert(kGGA * kGGB == kBlock, "one generator per thread");
-    // TMA destinations are 128-byte aligned
-    __shared__ __align__(128) float4 sp[kGHA][kGHB];
-    __shared__ __align__(128) float4 sst[4][kGGA][kGGB];  // stretch common + fired flag, per type
+    static_assert(sizeof(DomainParams) % 16 == 0, "DomainParams is staged in 16-byte pieces");
+    static_assert(kX || kMode == SOLVE_PLAIN, "the finalizing modes stage positions");
+    float4 (*const sp)[kGHB] = S.sp;
+    float4 (*const sst)[kGGA][kGGB] = S.sst;
+    float4 (*const sbd)[kGGA][kGGB] = S.sbd;
+    float4* const sgl = S.sgl;
+    float4* const sx = S.sx;
+    float4* const sslot = S.sslot;
+    float4* const ssup = S.ssup;
+    uint64_t& sbar = S.sbar;
+    DomainParams& sdom = S.sdom;
     // the generator's four stretch rest lengths are staged in sst[0] at the generator's own
     // slot (gx * kGGB + gy == tid): the thread reads them before it writes that slot
     float4* const sgr = &sst[0][0][0];
-    __shared__ float4 sbd[4][kGGA][kGGB];  // bending corner corrections + fired flag
-    __shared__ __align__(128) float4 sgl[kBlock];  // the particle's LRA rest distances, or the slot groups' boxes
-    __shared__ __align__(128) float4 sx[kBlock];   // the particle's position (finalizing modes)
-    __shared__ __align__(8) uint64_t sbar;         // TMA completion barrier
-    __shared__ float4 sslot[kGridLraCached];
-    __shared__ float4 ssup[4 * (kLraGroupsMax / kLraSuper)];  // the slot super-groups' boxes
-    __shared__ __align__(16) DomainParams sdom;
-    static_assert(sizeof(DomainParams) % 16 == 0, "DomainParams is staged in 16-byte pieces");
-    const GridTile tl = tiles[blockIdx.x];
     const int tid = (int)threadIdx.x;
     const int R = tl.res, V = R + 1, base = tl.p_begin;
     const int ns = tl.slot_count, s0 = tl.slot_begin;
@@ -968,6 +989,70 @@ k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__
     grid_particle_sum<kGGA, kGGB>(a, b, R, i, hx, hy, sst, sbd, pi, wi, ns, s0, &sgl[tid], sslot, sgl, ssup,
                                   gsize, ngroups, x0, slots, slots0, D.lrs, acc, cnt);
     apply_and_finalize<kMode>(D, tl.dom, i, pi, wi, acc, cnt, &sx[tid], pout, x, v, status);
+}
+
+template <int kMode, int kTA, int kTB, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks)
+k_grid_iter(const GridTile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+            const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ x,
+            float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ grest,
+            const float4* __restrict__ glra, const float4* __restrict__ slots,
+            const float4* __restrict__ slots0, int32_t* __restrict__ status,
+            const CUtensorMap* __restrict__ tmaps, int pin_sel)
+{
+    constexpr int kX = kMode == SOLVE_PLAIN ? 0 : 1;
+    __shared__ GridSmem<kTA, kTB, kX> S;
+    grid_tile_iteration<kMode, kTA, kTB, kX>(S, tiles[blockIdx.x], doms, pin, pout, x, v, x0, grest, glra, slots,
+                                             slots0, status, tmaps, pin_sel);
+}
+
+// ------------------------------------------------------------------ cluster-resident substep
+// All Jacobi iterations of one substep of small grid cloths in one launch: a cluster of
+// kClusterCtas blocks owns one cloth (tiles [first, end) of the tile table, block r of the
+// cluster takes tiles first + r, first + r + kClusterCtas, ...) and runs the iterations
+// in order, separated by the cluster's hardware barrier, whose release / acquire makes
+// every block's positions of one iteration visible to the whole cluster before the next
+// reads them.  No block waits on memory written by another cluster, and the launch's
+// blocks of a cluster are co-scheduled by the hardware, so there is no spin-wait.  Each
+// tile step is grid_tile_iteration (cp.async staging), so results are k_grid_iter's.
+constexpr int kClusterCtas = 16;
+
+__device__ __forceinline__ void cluster_barrier()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+template <int kTA, int kTB>
+__global__ void __launch_bounds__(kBlock, 1)
+k_grid_substep_cluster(const GridTile* __restrict__ tiles, const int2* __restrict__ cloth_tiles,
+                       const DomainParams* __restrict__ doms, float4* __restrict__ p0, float4* __restrict__ p1,
+                       float4* __restrict__ x, float4* __restrict__ v, const float4* __restrict__ x0,
+                       const float4* __restrict__ grest, const float4* __restrict__ glra,
+                       const float4* __restrict__ slots, const float4* __restrict__ slots0,
+                       int32_t* __restrict__ status, int pin0, int iterations, int last_substep)
+{
+    __shared__ GridSmem<kTA, kTB, 1> S;
+    const int2 range = cloth_tiles[blockIdx.x / kClusterCtas];
+    const int rank = (int)(blockIdx.x % kClusterCtas);
+    int pin = pin0;
+    for (int it = 0; it < iterations; ++it) {
+        const float4* pi = pin ? p1 : p0;
+        float4* po = pin ? p0 : p1;
+        for (int t = range.x + rank; t < range.y; t += kClusterCtas) {
+            __syncthreads();  // the previous tile step is done with the shared tile
+            if (it + 1 < iterations)
+                grid_tile_iteration<SOLVE_PLAIN, kTA, kTB, 1>(S, tiles[t], doms, pi, po, x, v, x0, grest, glra, slots,
+                                                           slots0, status, nullptr, pin);
+            else if (last_substep)
+                grid_tile_iteration<SOLVE_FINALIZE, kTA, kTB, 1>(S, tiles[t], doms, pi, po, x, v, x0, grest, glra,
+                                                              slots, slots0, status, nullptr, pin);
+            else
+                grid_tile_iteration<SOLVE_FINALIZE_PREDICT, kTA, kTB, 1>(S, tiles[t], doms, pi, po, x, v, x0, grest,
+                                                                      glra, slots, slots0, status, nullptr, pin);
+        }
+        cluster_barrier();
+        pin = 1 - pin;
+    }
 }
 
 template <int kPredict>
@@ -1183,6 +1268,80 @@ cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int mode)
     if (L.grid_variant < 0 || L.grid_variant >= kGridVariants) return cudaErrorInvalidValue;
     grid_iter_dispatch(L, pin, pout, mode, std::make_integer_sequence<int, kGridVariants>{});
     return cudaGetLastError();
+}
+
+// The substep's iterations through k_grid_substep_cluster: one cluster per grid cloth,
+// cloth_tiles[c] = its tile range in the tile table of the current variant.
+template <int v>
+static cudaError_t substep_cluster_variant(const Launch& L, const int2* cloth_tiles, int n_cloths, int pin,
+                                           int iterations, int last_sub)
+{
+    constexpr GridVariant g = kGridVariant[v];
+    const DeviceArrays& d = *L.d;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(kClusterCtas * n_cloths));
+    cfg.blockDim = dim3(kBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = L.st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kClusterCtas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_grid_substep_cluster<g.ta, g.tb>, d.gtiles, cloth_tiles, d.dom, d.p[0],
+                              d.p[1], d.x, d.v, d.x0, d.grest, d.glra, d.slots, d.slots0, d.status, pin, iterations,
+                              last_sub);
+}
+
+template <int... V>
+static cudaError_t substep_cluster_dispatch(const Launch& L, const int2* ct, int n, int pin, int its, int last,
+                                            std::integer_sequence<int, V...>)
+{
+    cudaError_t e = cudaErrorInvalidValue;
+    ((L.grid_variant == V ? (void)(e = substep_cluster_variant<V>(L, ct, n, pin, its, last)) : void()), ...);
+    return e;
+}
+
+cudaError_t launch_grid_substep_cluster(const Launch& L, const int2* cloth_tiles, int n_cloths, int pin,
+                                        int iterations, int last_sub)
+{
+    if (!L.n_gtiles || n_cloths <= 0 || iterations <= 0) return cudaSuccess;
+    if (L.grid_variant < 0 || L.grid_variant >= kGridVariants) return cudaErrorInvalidValue;
+    return substep_cluster_dispatch(L, cloth_tiles, n_cloths, pin, iterations, last_sub,
+                                    std::make_integer_sequence<int, kGridVariants>{});
+}
+
+// Whether this device runs clusters of kClusterCtas blocks of the substep kernel (a
+// non-portable size: it needs the kernel attribute and a GPC with that many free SMs).
+template <int TA, int TB>
+static bool cluster_kernel_fits()
+{
+    auto k = k_grid_substep_cluster<TA, TB>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return false;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kBlock);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kClusterCtas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    return cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n >= 1;
+}
+
+bool substep_clusters_supported()
+{
+    static int ok = -1;
+    if (ok < 0) {
+        ok = cluster_kernel_fits<7, 31>() && cluster_kernel_fits<15, 15>() && cluster_kernel_fits<3, 63>() ? 1 : 0;
+        (void)cudaGetLastError();  // a refused query leaves no sticky error
+    }
+    return ok == 1;
 }
 
 cudaError_t launch_finalize(const Launch& L, int pcur, int predict_next)

@@ -252,6 +252,16 @@ bool encode_grid_tmaps(CUtensorMap* dst, const float4* p0, const float4* p1, con
 }
 
 bool tile_loads_tma() { return g_tile_tma.load(); }
+
+namespace {
+std::atomic<bool> g_substep_clusters{true};
+}
+bool substep_clusters_enabled() { return g_substep_clusters.load(); }
+vt_status set_substep_clusters(bool on)
+{
+    g_substep_clusters.store(on);
+    return VT_OK;
+}
 vt_status set_tile_loads_tma(bool on)
 {
     g_tile_tma.store(on);
@@ -341,11 +351,40 @@ vt_status World::set_grid_variant(int variant)
                 "upload gtiles");
     n_gtiles = (int32_t)gt.size();
     grid_variant = variant;
+    {
+        const vt_status r = update_cluster_plan();
+        if (r != VT_OK) return r;
+    }
     if (gexec_) {  // a captured frame bakes in the tile count
         cudaGraphExecDestroy(gexec_);
         gexec_ = nullptr;
         gkey_[0] = -1;
     }
+    return VT_OK;
+}
+
+// Tile ranges of the grid cloths for the cluster-resident substep kernel, and whether this
+// world can use it: every domain solved by the tile kernel (no CSR domain has launches of
+// its own inside the iterations) and every cloth within kClusterMaxTiles tiles.
+vt_status World::update_cluster_plan()
+{
+    cluster_ok_ = false;
+    n_cluster_cloths_ = 0;
+    if (grid_doms_.empty() || n_stiles || n_btiles || (int32_t)grid_doms_.size() != n_domains) return VT_OK;
+    std::vector<int2> ranges;
+    int32_t t0 = 0;
+    for (auto& gd : grid_doms_) {
+        std::vector<GridTile> tmp;
+        grid_tiles_for(tmp, gd.first, hdom[gd.first], grid_variant);
+        if ((int32_t)tmp.size() > kClusterMaxTiles) return VT_OK;
+        ranges.push_back(make_int2(t0, t0 + (int32_t)tmp.size()));
+        t0 += (int32_t)tmp.size();
+    }
+    if (t0 != n_gtiles || !substep_clusters_supported()) return VT_OK;
+    VT_CUDA(cudaMemcpy(cloth_tiles_dev_, ranges.data(), ranges.size() * sizeof(int2), cudaMemcpyHostToDevice),
+            "upload cloth tile ranges");
+    n_cluster_cloths_ = (int32_t)ranges.size();
+    cluster_ok_ = true;
     return VT_OK;
 }
 
@@ -668,6 +707,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_st = A.take<int32_t>(1 + n_domains), o_pk = A.take<float>(3 * (size_t)N);
     const size_t o_ps = A.take<float4>(N), o_x0s = A.take<float4>(N);
     const size_t o_tm = A.take<CUtensorMap>(any_grid ? (size_t)kTmapsPerDomain * n_domains : 0);
+    const size_t o_ctl = A.take<int2>(n_domains);
     bytes = A.off;
     VT_CUDA(cudaMalloc(&arena_, A.off), "cudaMalloc(world)");
     char* base = (char*)arena_;
@@ -690,6 +730,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     d.grest = AT(float4, o_grest); d.glra = AT(float4, o_glra); d.packed = AT(float, o_pk);
     d.ps = AT(float4, o_ps); d.x0s = AT(float4, o_x0s);
     CUtensorMap* tmaps_dev = any_grid ? AT(CUtensorMap, o_tm) : nullptr;
+    cloth_tiles_dev_ = AT(int2, o_ctl);
 #undef AT
     auto up = [](void* dst, const void* src, size_t bytes_) -> cudaError_t {
         return bytes_ ? cudaMemcpy(dst, src, bytes_, cudaMemcpyHostToDevice) : cudaSuccess;
@@ -738,6 +779,10 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
         d.tmaps = tmaps_dev;
     }
     VT_CUDA(prepare_kernels(), "kernel attributes");
+    {
+        const vt_status r = update_cluster_plan();
+        if (r != VT_OK) return r;
+    }
     tuned_ = false;
     frames_ = 0;
     VT_CUDA(cudaMemset(d.status, 0, (1 + n_domains) * 4), "memset status");
@@ -941,6 +986,14 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
         VT_STAGE(ST_COLLIDE, launch_collide(L, pc, 1 - pc), "collide", pk);
         pc = 1 - pc;
         const bool last_sub = sub == a.substeps - 1;
+        if (cluster_ok_ && a.iterations > 0 && substep_clusters_enabled()) {
+            // small grid cloths: the substep's iterations in one launch of clusters
+            VT_STAGE(ST_GRID_ITER,
+                     launch_grid_substep_cluster(L, cloth_tiles_dev_, n_cluster_cloths_, pc, a.iterations,
+                                                 last_sub ? 1 : 0),
+                     "grid_iter", 1);
+            if (a.iterations % 2) pc = 1 - pc;
+        } else
         for (int it = 0; it < a.iterations; ++it) {
             if (n_btiles) VT_STAGE(ST_BEND, launch_bend(L, pc), "bend", bk);
             const int mode = it < a.iterations - 1 ? SOLVE_PLAIN

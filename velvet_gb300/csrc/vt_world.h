@@ -256,6 +256,19 @@ cudaError_t launch_pack_xyz(const float4* src, float* dst, int64_t n, cudaStream
 cudaError_t launch_grid_iter(const Launch& L, int pin, int pout, int final_mode);
 // One-time kernel attributes (call outside any stream capture).
 cudaError_t prepare_kernels();
+// All iterations of one substep of every grid cloth in one launch of clusters (one
+// cluster per cloth, cloth_tiles[c] its tile range); see k_grid_substep_cluster.
+cudaError_t launch_grid_substep_cluster(const Launch& L, const int2* cloth_tiles, int n_cloths, int pin,
+                                        int iterations, int last_sub);
+bool substep_clusters_supported();
+// Grid cloths of at most this many tiles (of the variant in use) take the cluster kernel:
+// one tile per block, a single round per iteration.  (With two rounds — a 64x64 cloth's 25
+// tiles of 15x15 on 16 blocks — each iteration pays the tile's dependent-latency chain
+// twice and the frame took 0.62 ms against 0.48 ms with one launch per iteration.)
+constexpr int kClusterMaxTiles = 16;
+// Whether small-cloth worlds run a substep's iterations as one cluster launch (default).
+bool substep_clusters_enabled();
+vt_status set_substep_clusters(bool on);
 
 cudaError_t launch_presdf_predict(const Launch& L, int pcur);
 cudaError_t launch_collide(const Launch& L, int pin, int pout);
