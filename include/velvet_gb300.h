@@ -482,8 +482,9 @@ vt_status vt_tuning_set_tile_loads(int32_t tma);
  * run all Jacobi iterations of a substep in one launch: a thread-block cluster of 16
  * blocks per cloth steps through its tiles and separates the iterations with the
  * cluster's hardware barrier (on = 1, the default), instead of one launch per iteration
- * (0).  Same results; applies to frames enqueued afterwards.  The reference launches each
- * constraint kernel once per iteration (Velvet/VtClothSolverGPU.hpp:90-96). */
+ * (0).  Same results; applies to frames enqueued, and CUDA graphs captured, afterwards (a
+ * solver or batch that already captured its frame graph keeps it).  The reference
+ * launches each constraint kernel once per iteration (Velvet/VtClothSolverGPU.hpp:90-96). */
 vt_status vt_tuning_set_substep_clusters(int32_t on);
 /* The shape in use by a solver / batch (after its first frame). */
 vt_status vt_solver_grid_tile(const vt_solver* s, int32_t* variant);
