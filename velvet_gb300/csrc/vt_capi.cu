@@ -782,8 +782,8 @@ vt_status vt_solver_debug_get(vt_solver* s, int32_t what, void* dst, uint64_t by
     switch (what) {
     case VT_DEBUG_PARTICLE_HASH: src = d.keys; need = 4 * n; break;
     case VT_DEBUG_PARTICLE_INDEX: src = d.vals; need = 4 * n; break;
-    case VT_DEBUG_CELL_START: src = d.cell_start; need = 4 * (T + 1); break;
-    case VT_DEBUG_CELL_END: src = d.cell_end; need = 4 * T; break;
+    case VT_DEBUG_CELL_START: need = 4 * (T + 1); break;
+    case VT_DEBUG_CELL_END: need = 4 * T; break;
     case VT_DEBUG_NEIGHBORS: src = d.nbr; need = 4 * n * (uint64_t)s->h.P.max_num_neighbors; break;
     case VT_DEBUG_PREDICTED: need = 12 * n; break;
     default: vt::set_error("unknown debug view"); return VT_ERR_INVALID_ARGUMENT;
@@ -792,6 +792,13 @@ vt_status vt_solver_debug_get(vt_solver* s, int32_t what, void* dst, uint64_t by
     VT_TRY_CUDA(cudaStreamSynchronize(s->stream), "sync");
     if (what == VT_DEBUG_PREDICTED) {
         if (n) VT_TRY_CUDA(cudaMemcpy2D(dst, 12, d.p[s->world.pcur], 16, 12, n, cudaMemcpyDeviceToHost), "copy");
+        return VT_OK;
+    }
+    if (what == VT_DEBUG_CELL_START || what == VT_DEBUG_CELL_END) {
+        // the device keeps (start, end) pairs; each view is one column of them
+        const char* col = reinterpret_cast<const char*>(d.cells) + (what == VT_DEBUG_CELL_END ? 4 : 0);
+        const uint64_t rows = what == VT_DEBUG_CELL_END ? T : T + 1;
+        if (rows) VT_TRY_CUDA(cudaMemcpy2D(dst, 4, col, 8, 4, rows, cudaMemcpyDeviceToHost), "copy");
         return VT_OK;
     }
     if (what == VT_DEBUG_NEIGHBORS && n) {

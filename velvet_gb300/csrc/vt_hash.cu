@@ -299,17 +299,17 @@ cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_s
 __global__ void __launch_bounds__(kBlock)
 k_cell_ranges_gather(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                      const float4* __restrict__ p, const float4* __restrict__ x0, int32_t n,
-                     uint32_t* __restrict__ cs, uint32_t* __restrict__ ce, float4* __restrict__ ps,
-                     float4* __restrict__ x0s, int32_t* __restrict__ status)
+                     uint2* __restrict__ cells, float4* __restrict__ ps, float4* __restrict__ x0s,
+                     int32_t* __restrict__ status)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
     if (t >= n) return;
     const uint32_t h = keys[t];
     if (t == 0 || keys[t - 1] != h) {
-        cs[h] = (uint32_t)t;
-        if (t > 0) ce[keys[t - 1]] = (uint32_t)t;
+        cells[h].x = (uint32_t)t;
+        if (t > 0) cells[keys[t - 1]].y = (uint32_t)t;
     }
-    if (t == n - 1) ce[h] = (uint32_t)n;
+    if (t == n - 1) cells[h].y = (uint32_t)n;
     const uint32_t id = vals[t];
     if (!VT_IN_RANGE(id, 0, n, status)) return;
     const float4 q = p[id];
@@ -321,8 +321,7 @@ cudaError_t launch_cell_ranges_gather(const DeviceArrays& d, int pin, int32_t n,
 {
     if (n <= 0) return cudaSuccess;
     k_cell_ranges_gather<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(d.keys, d.vals, d.p[pin], d.x0, n,
-                                                                      d.cell_start, d.cell_end, d.ps, d.x0s,
-                                                                      d.status);
+                                                                      d.cells, d.ps, d.x0s, d.status);
     return cudaGetLastError();
 }
 
@@ -392,8 +391,7 @@ __device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* 
 // pairs loaded three buckets at a time all ran slower — the walk is bound by load
 // latency, and sorted order with the highest occupancy gives the most shared bucket
 // reads.)
-__device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint32_t* __restrict__ cs,
-                                                       const uint32_t* __restrict__ ce,
+__device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint2* __restrict__ cells,
                                                        const float4* __restrict__ ps,
                                                        const float4* __restrict__ x0s,
                                                        uint32_t* __restrict__ out_base, uint32_t id_base,
@@ -424,9 +422,10 @@ __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint32_
         for (int b = 0; b < 3; ++b)
             for (int c = 0; c < 3; ++c) {
                 const uint32_t h = (uint32_t)table_base + abs_mod(hx[a] ^ hy[b] ^ hz[c], M, (uint32_t)table);
-                const uint32_t start = cs[h];
+                const uint2 range = cells[h];  // start and end in one load
+                const uint32_t start = range.x;
                 if (start == 0xffffffffu) continue;
-                uint32_t end = ce[h];
+                uint32_t end = range.y;
                 const uint32_t lim = start + (uint32_t)max_nbr;
                 if (lim < end) end = lim;
                 if (!VT_IN_RANGE(end, start, (long long)slot_end + 1, status)) continue;
@@ -466,8 +465,7 @@ struct PosF3 {
 
 __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
-                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
-                  const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
+                  const uint2* __restrict__ cells, const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
                   int32_t* __restrict__ status)
 {
     const Tile tl = tiles[blockIdx.x];
@@ -475,7 +473,7 @@ k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict
     if (t >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
     // a domain's sorted slots are its particle range
-    cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + nbr_offset(D), (uint32_t)D.p_begin,
+    cache_neighbors_sorted((uint32_t)t, cells, ps, x0s, nbr + nbr_offset(D), (uint32_t)D.p_begin,
                            (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
                            ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2, D.diameter2,
                            D.max_nbr, (uint32_t)(D.p_begin + D.p_count), status);
@@ -525,7 +523,7 @@ k_hash_keys_arena(const int32_t* __restrict__ pdom, const DomainParams* __restri
 __global__ void __launch_bounds__(kBlock)
 k_cell_ranges_arena(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                     const int32_t* __restrict__ pdom, const float4* __restrict__ p, const float4* __restrict__ x0,
-                    int32_t n, uint32_t sentinel, uint32_t* __restrict__ cs, uint32_t* __restrict__ ce,
+                    int32_t n, uint32_t sentinel, uint2* __restrict__ cells,
                     float4* __restrict__ ps, float4* __restrict__ x0s, int32_t* __restrict__ dslot)
 {
     const int t = blockIdx.x * kBlock + (int)threadIdx.x;
@@ -533,10 +531,10 @@ k_cell_ranges_arena(const uint32_t* __restrict__ keys, const uint32_t* __restric
     const uint32_t h = keys[t];
     if (h == sentinel) return;
     if (t == 0 || keys[t - 1] != h) {
-        cs[h] = (uint32_t)t;
-        if (t > 0) ce[keys[t - 1]] = (uint32_t)t;
+        cells[h].x = (uint32_t)t;
+        if (t > 0) cells[keys[t - 1]].y = (uint32_t)t;
     }
-    if (t == n - 1 || keys[t + 1] == sentinel) ce[h] = (uint32_t)(t + 1);
+    if (t == n - 1 || keys[t + 1] == sentinel) cells[h].y = (uint32_t)(t + 1);
     const uint32_t id = vals[t];
     const int32_t dom = pdom[id];
     if (t == 0 || pdom[vals[t - 1]] != dom) dslot[dom] = t;
@@ -547,7 +545,7 @@ k_cell_ranges_arena(const uint32_t* __restrict__ keys, const uint32_t* __restric
 
 __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors_arena(const int32_t* __restrict__ pdom, const DomainParams* __restrict__ doms,
-                        const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                        const uint2* __restrict__ cells,
                         const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
                         const int32_t* __restrict__ dslot, int32_t n_active, int32_t* __restrict__ status)
 {
@@ -555,7 +553,7 @@ k_cache_neighbors_arena(const int32_t* __restrict__ pdom, const DomainParams* __
     if (t >= n_active) return;
     const int32_t dom = pdom[__float_as_uint(ps[t].w)];
     const DomainParams& D = doms[dom];
-    cache_neighbors_sorted((uint32_t)t, cs, ce, ps, x0s, nbr + nbr_offset(D), (uint32_t)D.p_begin,
+    cache_neighbors_sorted((uint32_t)t, cells, ps, x0s, nbr + nbr_offset(D), (uint32_t)D.p_begin,
                            (uint32_t)dslot[dom], D.p_count, D.table_base, D.table_size,
                            ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2, D.diameter2,
                            D.max_nbr, (uint32_t)n_active, status);
@@ -566,17 +564,17 @@ cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pi
                               uint64_t* launches)
 {
     if (hw <= 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(d.cell_start, 0xff, sizeof(uint32_t) * (size_t)sentinel, st);
+    cudaError_t e = cudaMemsetAsync(d.cells, 0xff, sizeof(uint2) * (size_t)sentinel, st);
     if (e != cudaSuccess) return e;
     const int blocks = (hw + kBlock - 1) / kBlock;
     k_hash_keys_arena<<<blocks, kBlock, 0, st>>>(pdom, d.dom, d.p[pin], d.keys, d.vals, hw, sentinel);
     e = radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot, hw, bits, st, d.status);
     if (e != cudaSuccess) return e;
     k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, d.vals, pdom, d.p[pin], d.x0, hw, sentinel,
-                                                   d.cell_start, d.cell_end, d.ps, d.x0s, d.dslot);
+                                                   d.cells, d.ps, d.x0s, d.dslot);
     if (n_active > 0)
         k_cache_neighbors_arena<<<(n_active + kBlock - 1) / kBlock, kBlock, 0, st>>>(
-            pdom, d.dom, d.cell_start, d.cell_end, d.ps, d.x0s, d.nbr, d.dslot, n_active, d.status);
+            pdom, d.dom, d.cells, d.ps, d.x0s, d.nbr, d.dslot, n_active, d.status);
     const int passes = (hw > 1 && bits > 0) ? (bits + 7) / 8 : 0;
     if (launches) *launches += 3 + 3 * (uint64_t)passes;
     return cudaGetLastError();
@@ -595,7 +593,7 @@ cudaError_t launch_cache_neighbors(const Launch& L, int pin)
     if (!L.n_ptiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
     (void)pin;  // positions come sorted from launch_cell_ranges_gather
-    k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.cell_start, d.cell_end, d.ps,
+    k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.cells, d.ps,
                                                        d.x0s, d.nbr, d.status);
     return cudaGetLastError();
 }

@@ -451,7 +451,7 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     s->d.keys = (uint32_t*)take(a4); s->d.vals = (uint32_t*)take(a4);
     s->d.keys_tmp = (uint32_t*)take(a4); s->d.vals_tmp = (uint32_t*)take(a4);
     s->d.hist = (uint32_t*)take(hist); s->d.digit_tot = (uint32_t*)take(256 * 4);
-    s->d.cell_start = (uint32_t*)take(cells); s->d.cell_end = (uint32_t*)take(cells);
+    s->d.cells = (uint2*)take(2 * cells);
     s->d.nbr = (uint32_t*)take(nbr);
     s->d.packed = (float*)take(a12);
     s->d.dom = (vt::DomainParams*)take(M * sizeof(vt::DomainParams));

@@ -7,7 +7,7 @@
 //   presdf_predict                           CollideSDF(x, frameDt) + Predict(substep 0)
 //   for each substep s:
 //     if self-collision and s % interleavedHash == 0:
-//        fill cell_start 0xff, hash_keys, radix sort, cell_ranges_gather
+//        fill the cell ranges 0xff, hash_keys, radix sort, cell_ranges_gather
 //        (+ sorted copies of the positions), cache_neighbors
 //     collide                                CollideParticles + ApplyDeltas + CollideSDF
 //     for each iteration:                    Stretch + Attach + Bending + ApplyDeltas
@@ -697,7 +697,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_k = A.take<uint32_t>(N), o_vl = A.take<uint32_t>(N);
     const size_t o_kt = A.take<uint32_t>(N), o_vt = A.take<uint32_t>(N);
     const size_t o_h = A.take<uint32_t>(radix_hist_words((int32_t)N)), o_dt = A.take<uint32_t>(256);
-    const size_t o_cs = A.take<uint32_t>(TK), o_ce = A.take<uint32_t>(TK), o_nb = A.take<uint32_t>(NW);
+    const size_t o_cs = A.take<uint2>(TK), o_nb = A.take<uint32_t>(NW);
     const size_t o_dom = A.take<DomainParams>(n_domains), o_col = A.take<ColliderDev>(C);
     const size_t o_pt = A.take<Tile>(pt.size()), o_bt = A.take<Tile>(bt.size());
     const size_t o_stt = A.take<Tile>(st_tiles.size()), o_gt = A.take<GridTile>(gtiles_cap_);
@@ -723,7 +723,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     d.keys = AT(uint32_t, o_k); d.vals = AT(uint32_t, o_vl);
     d.keys_tmp = AT(uint32_t, o_kt); d.vals_tmp = AT(uint32_t, o_vt);
     d.hist = AT(uint32_t, o_h); d.digit_tot = AT(uint32_t, o_dt);
-    d.cell_start = AT(uint32_t, o_cs); d.cell_end = AT(uint32_t, o_ce); d.nbr = AT(uint32_t, o_nb);
+    d.cells = AT(uint2, o_cs); d.nbr = AT(uint32_t, o_nb);
     d.dom = AT(DomainParams, o_dom); d.col = AT(ColliderDev, o_col);
     d.ptiles = AT(Tile, o_pt); d.btiles = AT(Tile, o_bt); d.status = AT(int32_t, o_st);
     d.stiles = AT(Tile, o_stt); d.gtiles = AT(GridTile, o_gt); d.gptiles = AT(Tile, o_gpt);
@@ -755,8 +755,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     VT_CUDA(up(d.tri, htri.data(), TR * 16), "upload tri");
     VT_CUDA(up(d.tn_off, tn.off.data(), (N + 1) * 4), "upload tn_off");
     VT_CUDA(up(d.tn_ent, tn.ent.data(), tn.ent.size() * 4), "upload tn_ent");
-    VT_CUDA(cudaMemset(d.cell_start, 0xff, (size_t)TK * 4), "memset cell_start");
-    VT_CUDA(cudaMemset(d.cell_end, 0, (size_t)TK * 4), "memset cell_end");
+    VT_CUDA(cudaMemset(d.cells, 0xff, (size_t)TK * sizeof(uint2)), "memset cells");
     VT_CUDA(cudaMemset(d.nbr, 0xff, (size_t)NW * 4), "memset nbr");
     VT_CUDA(up(d.ptiles, pt.data(), pt.size() * sizeof(Tile)), "upload ptiles");
     VT_CUDA(up(d.btiles, bt.data(), bt.size() * sizeof(Tile)), "upload btiles");
@@ -974,7 +973,7 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
     VT_STAGE(ST_PRESDF_PREDICT, launch_presdf_predict(L, pc), "presdf_predict", pk);
     for (int sub = 0; sub < a.substeps; ++sub) {
         if (any_self && sub % ih == 0) {
-            VT_CUDA(cudaMemsetAsync(d.cell_start, 0xff, (size_t)total_keys * 4, st), "memset cells");
+            VT_CUDA(cudaMemsetAsync(d.cells, 0xff, (size_t)total_keys * sizeof(uint2), st), "memset cells");
             VT_STAGE(ST_HASH_KEYS, launch_hash_keys(L, pc), "hash_keys", pk);
             VT_STAGE(ST_RADIX_SORT,
                      radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot,

@@ -20,7 +20,7 @@
 //               (constraint, corner): correction + fired flag; bd_off/bd_ent CSR of
 //               corner slots per particle in constraint order
 //   normals     tn_off/tn_ent CSR of triangles per vertex; tri uint4 per triangle
-//   hash        keys/vals (sorted pairs), cell_start (sum of (T_d + 1)), cell_end,
+//   hash        keys/vals (sorted pairs), cells (start, end) per bucket (sum of (T_d + 1)),
 //               neighbours (max_nbr * n_d per domain, column-major inside a domain, in
 //               sorted-slot order: the list of the particle in the domain's r-th sorted
 //               slot is column r, so the walk that writes the lists and the collision
@@ -195,7 +195,10 @@ struct DeviceArrays {
     // hash
     uint32_t *keys = nullptr, *vals = nullptr, *keys_tmp = nullptr, *vals_tmp = nullptr;
     uint32_t *hist = nullptr, *digit_tot = nullptr;
-    uint32_t *cell_start = nullptr, *cell_end = nullptr, *nbr = nullptr;
+    // cell ranges of the solver's hash: cells[h] = (start, end) of bucket h, start
+    // 0xffffffff when empty, so one 8-byte load answers a bucket probe
+    uint2* cells = nullptr;
+    uint32_t* nbr = nullptr;
     // tables
     DomainParams* dom = nullptr;
     ColliderDev* col = nullptr;
