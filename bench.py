@@ -680,6 +680,56 @@ def serving_legs(args, duration: float, plain_seconds: float) -> tuple[dict, dic
     return served, plain
 
 
+def served_mix_leg(args, wl, plain_value: float | None) -> dict:
+    """The served form on the mixed-size workload itself: every cloth of the mix arrives at
+    once as a request of --served-mix-frames frames (registered beforehand, untimed), the
+    server admits them under its budget and active-particle cap and runs them by continuous
+    batching until the last one finishes.  Reports particle-iterations/s over the wall
+    time, the frame latency distribution and the ratio to the plain solver on the same
+    mix."""
+    import torch
+
+    import velvet_gb300 as vg
+
+    frames = args.served_mix_frames
+    S, It = wl.substeps, wl.iterations
+    solvers = [new_solver(spec) for spec in wl.cloths]
+    stream = torch.cuda.Stream()
+    srv = vg.ClothServer(int(args.budget_gb * (1 << 30)), max_cloths=2 * len(wl.cloths),
+                         max_active_particles=args.max_active_particles, substeps=S, iterations=It)
+    # warm-up: one small cloth through the whole path
+    srv.submit(solvers[0], 2)
+    while srv.tick(stream).active or srv.stats().requests_done < 1:
+        pass
+    base = srv.stats()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ids = [srv.submit(s, frames) for s in solvers]
+    ticks = 0
+    while True:
+        info = srv.tick(stream)
+        ticks += 1
+        if info.active == 0 and info.queued == 0:
+            break
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    done = sum(1 for r in ids if srv.poll(r)[0] == 2)
+    pits = st.particle_iterations - base.particle_iterations
+    out = {"value": pits / wall, "unit": UNIT, "wall_s": wall, "ticks": ticks, "requests": len(ids),
+           "completed": done, "frames_per_request": frames,
+           "p50_frame_ms": st.p50_frame_ms, "p99_frame_ms": st.p99_frame_ms,
+           "max_active_particles": args.max_active_particles,
+           "what": "every cloth of the mix submitted at once (registered, untimed), admitted under the cap, "
+                   "run to completion by continuous batching; frame latency = a tick's event-timed GPU time, "
+                   "weighted by its requests"}
+    if plain_value:
+        out["over_plain"] = out["value"] / plain_value
+    srv.close()
+    for s in solvers:
+        s.close()
+    return out
+
+
 def run_serving(args) -> None:
     """--workload serving: the served and plain legs for --duration / --plain-seconds."""
     import torch
@@ -734,7 +784,9 @@ def main() -> None:
                     help="batched run: seconds of the served leg (Poisson stream at --rate)")
     ap.add_argument("--served-plain-seconds", type=float, default=8.0,
                     help="batched run: seconds of the served leg's plain comparison")
-    ap.add_argument("--no-served", action="store_true", help="skip the served leg")
+    ap.add_argument("--no-served", action="store_true", help="skip the served legs")
+    ap.add_argument("--served-mix-frames", type=int, default=6,
+                    help="frames per request when the served form runs the mixed-size workload")
     ap.add_argument("--tile-loads", choices=["tma", "cp_async"], default="cp_async",
                     help="how the grid kernel stages its tiles (same results)")
     ap.add_argument("--substep-clusters", choices=["on", "off"], default="on",
@@ -960,6 +1012,11 @@ def main() -> None:
         for s, _, _ in solvers:
             s.close()
 
+    # the served form on the mixed-size workload itself, against the plain solver on it
+    served_mix = None
+    if rank == 0 and world == 1 and not args.no_served:
+        served_mix = served_mix_leg(args, wl, plain["value"] if plain else None)
+
     # the served form on a bounded Poisson stream, and its plain comparison (one GPU)
     served = None
     if rank == 0 and world == 1 and not args.no_served:
@@ -1020,6 +1077,7 @@ def main() -> None:
             "cpu_baseline": cpu,
             "cpu_reference_cpu_solver": cpu_ref_solver,
             "cpu_reference_cpu_solver_all_cores": cpu_ref_solver_all,
+            "served_mix": served_mix,
             "served": served,
             "exact_build": exact,
             "host": host_info(),
