@@ -780,23 +780,24 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
                                                   int& cnt)
 {
     const float nw = -wi;
-#define VT_TAKE(s4, scale)                          \
-    do {                                            \
-        const float4 s_ = (s4);                     \
-        if (s_.w != 0.0f) {                         \
-            acc3(acc, mk3(s_.x, s_.y, s_.z) * (scale)); \
-            cnt++;                                  \
-        }                                           \
+    // Branch-free: a constraint that does not exist (outside the cloth) or did not fire is
+    // stored as all zeros, so its term adds +-0, which leaves the sum's bits unchanged (the
+    // sum starts at +0 and an exact IEEE sum is never -0), and the count takes the flag.
+#define VT_TAKE(s4, scale)                              \
+    do {                                                \
+        const float4 s_ = (s4);                         \
+        acc3(acc, mk3(s_.x, s_.y, s_.z) * (scale));     \
+        cnt += s_.w != 0.0f ? 1 : 0;                    \
     } while (0)
     // stretch, constraint order: generators (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
-    if (a >= 1 && b >= 1) VT_TAKE(sst[2][gx - 1][gy - 1], wi);  // t2, second endpoint
-    if (a >= 1) VT_TAKE(sst[1][gx - 1][gy], wi);                // t1, second endpoint
-    if (a >= 1 && b < R) VT_TAKE(sst[3][gx - 1][gy], wi);       // t3, second endpoint
-    if (b >= 1) VT_TAKE(sst[0][gx][gy - 1], wi);                // t0, second endpoint
-    if (b >= 1 && a < R) VT_TAKE(sst[3][gx][gy - 1], nw);       // t3, first endpoint
-    if (b < R) VT_TAKE(sst[0][gx][gy], nw);                     // t0, first endpoint
-    if (a < R) VT_TAKE(sst[1][gx][gy], nw);                     // t1, first endpoint
-    if (a < R && b < R) VT_TAKE(sst[2][gx][gy], nw);            // t2, first endpoint
+    VT_TAKE(sst[2][gx - 1][gy - 1], wi);  // t2, second endpoint
+    VT_TAKE(sst[1][gx - 1][gy], wi);      // t1, second endpoint
+    VT_TAKE(sst[3][gx - 1][gy], wi);      // t3, second endpoint
+    VT_TAKE(sst[0][gx][gy - 1], wi);      // t0, second endpoint
+    VT_TAKE(sst[3][gx][gy - 1], nw);      // t3, first endpoint
+    VT_TAKE(sst[0][gx][gy], nw);          // t0, first endpoint
+    VT_TAKE(sst[1][gx][gy], nw);          // t1, first endpoint
+    VT_TAKE(sst[2][gx][gy], nw);          // t2, first endpoint
 #undef VT_TAKE
     // long-range attachments, slot order; pairs that cannot fire skip their square roots
     if (ns) {
@@ -824,19 +825,18 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
             }
         }
     }
-    // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
-#define VT_CORNER(c4)                     \
-    do {                                  \
-        const float4 c_ = (c4);           \
-        if (c_.w != 0.0f) {               \
-            acc3(acc, xyz(c_));           \
-            cnt++;                        \
-        }                                 \
+    // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b);
+    // branch-free as the stretch terms above
+#define VT_CORNER(c4)                       \
+    do {                                    \
+        const float4 c_ = (c4);             \
+        acc3(acc, xyz(c_));                 \
+        cnt += c_.w != 0.0f ? 1 : 0;        \
     } while (0)
-    if (a >= 1 && b >= 1) VT_CORNER(sbd[1][gx - 1][gy - 1]);
-    if (a >= 1 && b < R) VT_CORNER(sbd[3][gx - 1][gy]);
-    if (a < R && b >= 1) VT_CORNER(sbd[2][gx][gy - 1]);
-    if (a < R && b < R) VT_CORNER(sbd[0][gx][gy]);
+    VT_CORNER(sbd[1][gx - 1][gy - 1]);
+    VT_CORNER(sbd[3][gx - 1][gy]);
+    VT_CORNER(sbd[2][gx][gy - 1]);
+    VT_CORNER(sbd[0][gx][gy]);
 #undef VT_CORNER
 }
 
