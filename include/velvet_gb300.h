@@ -528,7 +528,7 @@ vt_status vt_hash_objects(uint32_t* particle_hash, uint32_t* particle_index,
  * device allocation, or a real-time frame loop where cudaMalloc / cudaFree would
  * synchronise the device and stall the frame.  vt_hash_objects allocates its sort
  * scratch on first use; this variant uses a fixed scratch array compiled into the
- * library instead (about 2.2 MB, held on every GPU that loads the library until the
+ * library instead (about 2.4 MB, held on every GPU that loads the library until the
  * process exits), so it accepts at most VT_HASH_NOALLOC_MAX_OBJECTS objects and returns
  * VT_ERR_CAPACITY above that.  Same arguments, same outputs as vt_hash_objects.
  *   - The first call on each device looks up the scratch array's device address (a

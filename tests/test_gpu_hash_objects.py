@@ -86,3 +86,16 @@ def test_hash_objects_empty_and_single():
     _check(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), 0.05, 16, 64, 0.03)
     one = np.array([[0.01, -0.02, 0.03]], np.float32)
     _check(one, one, 0.05, 2, 64, 0.03)
+
+
+@pytest.mark.parametrize("T", [200, 40_000, 300_000, (1 << 25) + 1])
+def test_hash_objects_sort_passes_one_to_four(T):
+    """Tables whose key widths (8, 16, 19 and 26 bits) make the radix sort run one, two,
+    three and four digit passes: an odd count starts from the temporaries, and every
+    count must leave the sorted pairs in the caller's buffers."""
+    rng = np.random.default_rng(T)
+    n = 70_000  # 18 sort tiles, so each pass's look-back crosses tiles
+    pos = rng.uniform(-1.0, 1.0, (n, 3)).astype(np.float32)
+    pos[:, 1] *= 0.2
+    orig = (pos + rng.normal(0.0, 0.05, (n, 3))).astype(np.float32)
+    _check(pos, orig, 0.04, T, 32, 0.02)

@@ -897,7 +897,7 @@ vt_status vt_hash_objects(uint32_t* particle_hash, uint32_t* particle_index, uin
     VT_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     VT_CHECK(dev >= 0 && dev < 64, VT_ERR_STATE, "device ordinal beyond 64");
     const int32_t n = (int32_t)hp->num_objects;
-    const size_t need = 2 * (size_t)(n > 0 ? n : 1) + vt::radix_hist_words(n) + 256;
+    const size_t need = 2 * (size_t)(n > 0 ? n : 1) + vt::radix_hist_words(n);
     std::lock_guard<std::mutex> lock(g_hash_mu);
     HashScratch& S = g_hash_scratch[dev];
     if (S.words < need) {
@@ -910,9 +910,8 @@ vt_status vt_hash_objects(uint32_t* particle_hash, uint32_t* particle_index, uin
     uint32_t* kt = S.buf;
     uint32_t* vt_ = kt + (n > 0 ? n : 1);
     uint32_t* hist = vt_ + (n > 0 ? n : 1);
-    uint32_t* dtot = hist + vt::radix_hist_words(n);
     VT_TRY_CUDA(vt::hash_objects_f3(particle_hash, particle_index, cell_start, cell_end, neighbors,
-                                    positions, original_positions, *hp, kt, vt_, hist, dtot,
+                                    positions, original_positions, *hp, kt, vt_, hist,
                                     (cudaStream_t)stream),
                 "hash_objects");
     return VT_OK;

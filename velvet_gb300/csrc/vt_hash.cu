@@ -6,9 +6,10 @@
 //           ix = (int)floor(x / cellSpacing) with IEEE division (no reciprocal),
 //           int32 products wrapping;
 //   sort  = stable by key (the reference uses cub::DeviceRadixSort::SortPairs; here a
-//           hand-written LSD radix sort: per-tile digit histograms, per-digit scan over
-//           tiles, then a scatter whose ranks come from warp match-any + per-warp
-//           counters, so equal digits keep index order);
+//           hand-written LSD radix sort in the single-sweep form: one count of every
+//           pass's digits, then per pass one kernel whose tiles rank their pairs with
+//           warp match-any + per-warp counters, so equal digits keep index order, and
+//           find their output offsets by a decoupled look-back over earlier tiles);
 //   cells = cellStart[h] / cellEnd[h] of every occupied bucket, 0xffffffff elsewhere;
 //   lists = 27 buckets in x, y, z loop order, at most maxNumNeighbors entries read per
 //           bucket, pairs kept if |p_i - p_j|^2 < cellSpacing^2 and the initial
@@ -82,33 +83,71 @@ k_hash_keys_f3(const float* __restrict__ pos, int32_t n, float sp, int32_t table
 }
 
 // ------------------------------------------------------------------ radix sort
+// A stable LSD radix sort in the single-sweep form (chained scan with decoupled look-back,
+// Merrill and Garland 2016; its radix-sort use, Adinets and Merrill 2022): one kernel
+// counts the digits of every pass over all keys at once, then one kernel per pass ranks
+// each 4096-pair tile in shared memory and learns where its digits start from the
+// tiles before it through per-(tile, digit) words published in global memory, so no
+// per-tile histogram and no separate scan pass is needed.  Tiles take their ids from an
+// atomic counter in the order their blocks start, so a tile only ever waits on tiles
+// whose blocks are already running, and every wait is bounded.
 static constexpr int kRsItems = 16;
 static constexpr int kRsWarps = kBlock / 32;
 static constexpr int kRsTile = kBlock * kRsItems;  // 4096 pairs per tile
+static_assert(kRsTile == kRadixTileItems, "tile size shared with the scratch-size formula");
+static constexpr int kRsMaxPasses = 4;             // 32-bit keys in 8-bit digits
+// hist layout (words): digit counts of pass p at [256 p, 256 p + 256); the tile counter of
+// pass p at kRsCounters + p; the look-back word of (pass p, tile i, digit d) at
+// kRsLookBase + (p * ntiles + i) * 256 + d.
+static constexpr size_t kRsCounters = (size_t)kRsMaxPasses * 256, kRsLookBase = kRsCounters + 256;
+// look-back word: flag in the top two bits, a count below (counts stay under 2^30)
+static constexpr uint32_t kRsAggregate = 1u << 30, kRsPrefix = 2u << 30, kRsCountMask = (1u << 30) - 1;
+static constexpr int kRsLookTries = 1 << 21;
 
-size_t radix_hist_words(int32_t n)
+static_assert(kRsLookBase == kRadixScratchHead, "scratch head shared with the scratch-size formula");
+
+int radix_passes(int32_t n, int32_t bits) { return (n > 1 && bits > 0) ? (bits + 7) / 8 : 0; }
+
+int radix_launches(int32_t n, int32_t bits)
 {
-    const int64_t tiles = (n + kRsTile - 1) / kRsTile;
-    return (size_t)(tiles > 0 ? tiles : 1) * 256 + 256;
+    const int passes = radix_passes(n, bits);
+    return passes ? 1 + passes : 0;
 }
 
-__global__ void __launch_bounds__(kBlock)
-k_rs_upsweep(const uint32_t* __restrict__ keys, int32_t n, int shift, int nbits,
-             uint32_t* __restrict__ hist, int32_t ntiles)
+__device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t* a)
 {
-    __shared__ uint32_t h[256];
-    const int ndig = 1 << nbits;
-    for (int k = threadIdx.x; k < ndig; k += kBlock) h[k] = 0;
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_gpu(uint32_t* a, uint32_t v)
+{
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+
+// Digit counts of all passes in one read of the keys.
+__global__ void __launch_bounds__(kBlock)
+k_rs_count(const uint32_t* __restrict__ keys, int32_t n, int passes, int per, int bits,
+           uint32_t* __restrict__ hist)
+{
+    __shared__ uint32_t h[kRsMaxPasses][256];
+    for (int k = threadIdx.x; k < kRsMaxPasses * 256; k += kBlock) (&h[0][0])[k] = 0;
     __syncthreads();
-    const uint32_t mask = (uint32_t)ndig - 1;
-    const int base = blockIdx.x * kRsTile;
+    const int stride = gridDim.x * kBlock;
 #pragma unroll 4
-    for (int j = 0; j < kRsItems; ++j) {
-        const int idx = base + j * kBlock + (int)threadIdx.x;
-        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & mask], 1u);
+    for (int idx = blockIdx.x * kBlock + (int)threadIdx.x; idx < n; idx += stride) {
+        const uint32_t key = keys[idx];
+        for (int p = 0; p < passes; ++p) {
+            const int shift = p * per, nb = min(per, bits - shift);
+            atomicAdd(&h[p][(key >> shift) & ((1u << nb) - 1u)], 1u);
+        }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < ndig; k += kBlock) hist[(size_t)k * ntiles + blockIdx.x] = h[k];
+    for (int k = threadIdx.x; k < passes * 256; k += kBlock) {
+        const uint32_t c = (&h[0][0])[k];
+        if (c) atomicAdd(&hist[k], c);
+    }
 }
 
 // Block-wide exclusive scan of one value per thread (kBlock threads); returns the
@@ -137,48 +176,29 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
     return wpre + incl - v;
 }
 
-// One block per digit: exclusive scan of that digit's counts over the tiles.
+// One pass: rank a tile's pairs by digit (stable), find each digit's output start from
+// the global digit counts and the look-back over earlier tiles, and scatter.
 __global__ void __launch_bounds__(kBlock)
-k_rs_scan(uint32_t* __restrict__ hist, int32_t ntiles, uint32_t* __restrict__ digit_tot)
-{
-    uint32_t* row = hist + (size_t)blockIdx.x * ntiles;
-    uint32_t carry = 0;
-    for (int base = 0; base < ntiles; base += kBlock) {
-        const int idx = base + (int)threadIdx.x;
-        const uint32_t v = idx < ntiles ? row[idx] : 0u;
-        uint32_t tot;
-        const uint32_t ex = block_exclusive_scan(v, &tot);
-        if (idx < ntiles) row[idx] = carry + ex;
-        carry += tot;
-    }
-    if (threadIdx.x == 0) digit_tot[blockIdx.x] = carry;
-}
-
-__global__ void __launch_bounds__(kBlock)
-k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int32_t n, int shift,
-               int nbits, const uint32_t* __restrict__ hist, const uint32_t* __restrict__ digit_tot,
-               int32_t ntiles, int32_t* __restrict__ status)
+k_rs_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+              uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int32_t n, int pass, int shift,
+              int nbits, uint32_t* __restrict__ hist, int32_t ntiles, int32_t* __restrict__ status)
 {
     __shared__ uint32_t off[256];   // the tile's first output position per digit
     __shared__ uint32_t lofs[256];  // the digit's first slot in the tile's sorted copy
     __shared__ uint32_t wcnt[kRsWarps][256];
     __shared__ uint32_t sk[kRsTile], sv[kRsTile];  // the tile's pairs in output order
+    __shared__ int32_t tile_s;
     const int ndig = 1 << nbits;
     const uint32_t mask = (uint32_t)ndig - 1;
-    {
-        const uint32_t t = (int)threadIdx.x < ndig ? digit_tot[threadIdx.x] : 0u;
-        uint32_t tot;
-        const uint32_t ex = block_exclusive_scan(t, &tot);
-        if ((int)threadIdx.x < ndig)
-            off[threadIdx.x] = ex + hist[(size_t)threadIdx.x * ntiles + blockIdx.x];
-    }
+    if (threadIdx.x == 0) tile_s = (int32_t)atomicAdd(&hist[kRsCounters + pass], 1u);
     for (int k = threadIdx.x; k < kRsWarps * 256; k += kBlock) (&wcnt[0][0])[k] = 0;
     __syncthreads();
+    const int tile = tile_s;
+    if (tile >= ntiles) return;  // not reached: the grid has ntiles blocks
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1u;
-    const int wbase = blockIdx.x * kRsTile + warp * (32 * kRsItems);
+    const int wbase = tile * kRsTile + warp * (32 * kRsItems);
     uint32_t mk[kRsItems], mv[kRsItems], mr[kRsItems];
 #pragma unroll
     for (int j = 0; j < kRsItems; ++j) {
@@ -198,7 +218,7 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
         mr[j] = rank;
     }
     __syncthreads();
-    uint32_t run = 0;
+    uint32_t run = 0;  // the tile's count of digit threadIdx.x
     if ((int)threadIdx.x < ndig) {
 #pragma unroll
         for (int w = 0; w < kRsWarps; ++w) {
@@ -207,10 +227,37 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
             run += c;
         }
     }
-    {
-        uint32_t tot;
-        const uint32_t lex = block_exclusive_scan(run, &tot);
-        if ((int)threadIdx.x < ndig) lofs[threadIdx.x] = lex;
+    uint32_t tot;
+    const uint32_t lex = block_exclusive_scan(run, &tot);
+    const uint32_t gex = block_exclusive_scan((int)threadIdx.x < ndig ? hist[(size_t)pass * 256 + threadIdx.x] : 0u, &tot);
+    if ((int)threadIdx.x < ndig) {
+        lofs[threadIdx.x] = lex;
+        uint32_t* look = hist + kRsLookBase + (size_t)pass * ntiles * 256 + threadIdx.x;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            st_relaxed_gpu(look, kRsPrefix | run);
+        } else {
+            st_relaxed_gpu(look + (size_t)tile * 256, kRsAggregate | run);
+            int j = tile - 1, tries = 0;
+            while (true) {
+                const uint32_t v = ld_relaxed_gpu(look + (size_t)j * 256);
+                if ((v & ~kRsCountMask) == 0) {  // tile j has not published yet
+                    if (++tries > kRsLookTries) {
+                        // report it (the sync calls return VT_ERR_TIMEOUT); positions stay
+                        // below the true ones, so every store below stays in bounds
+                        if (status) atomicOr(status, VT_STATUS_TIMEOUT);
+                        break;
+                    }
+                    if (tries > 64) __nanosleep(64);
+                    continue;
+                }
+                excl += v & kRsCountMask;
+                if ((v & kRsPrefix) || j == 0) break;
+                --j;
+            }
+            st_relaxed_gpu(look + (size_t)tile * 256, kRsPrefix | (excl + run));
+        }
+        off[threadIdx.x] = gex + excl;
     }
     __syncthreads();
     // the tile's pairs into shared memory in (digit, stable rank) order, then written out
@@ -227,7 +274,7 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
         }
     }
     __syncthreads();
-    const int count = min(kRsTile, n - (int)blockIdx.x * kRsTile);
+    const int count = min(kRsTile, n - tile * kRsTile);
     for (int t = threadIdx.x; t < count; t += kBlock) {
         const uint32_t key = sk[t];
         const uint32_t d = (key >> shift) & mask;
@@ -239,33 +286,31 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
 }
 
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
-                             uint32_t* hist, uint32_t* digit_tot, int32_t n, int32_t bits,
-                             cudaStream_t st, int32_t* status)
+                             uint32_t* hist, int32_t n, int32_t bits, cudaStream_t st, int32_t* status)
 {
-    if (n <= 1 || bits <= 0) return cudaSuccess;
-    const int passes = (bits + 7) / 8;
+    const int passes = radix_passes(n, bits);
+    if (!passes) return cudaSuccess;
+    if (passes > kRsMaxPasses || n > (int32_t)kRsCountMask) return cudaErrorInvalidValue;
     const int per = (bits + passes - 1) / passes;
     const int32_t ntiles = (n + kRsTile - 1) / kRsTile;
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * (kRsLookBase + (size_t)passes * ntiles * 256), st);
+    if (e != cudaSuccess) return e;
+    // an odd number of passes starts from the temporaries, so the result lands in keys / vals
     uint32_t *ki = keys, *vi = vals, *ko = keys_tmp, *vo = vals_tmp;
+    if (passes % 2) {
+        ki = keys_tmp; vi = vals_tmp; ko = keys; vo = vals;
+    }
+    k_rs_count<<<ntiles < 1024 ? ntiles : 1024, kBlock, 0, st>>>(ki, n, passes, per, bits, hist);
     int shift = 0;
     for (int ps = 0; ps < passes; ++ps) {
         const int nb = (bits - shift) < per ? (bits - shift) : per;
-        k_rs_upsweep<<<ntiles, kBlock, 0, st>>>(ki, n, shift, nb, hist, ntiles);
-        k_rs_scan<<<1 << nb, kBlock, 0, st>>>(hist, ntiles, digit_tot);
-        k_rs_downsweep<<<ntiles, kBlock, 0, st>>>(ki, vi, ko, vo, n, shift, nb, hist, digit_tot, ntiles, status);
+        k_rs_onesweep<<<ntiles, kBlock, 0, st>>>(ki, vi, ko, vo, n, ps, shift, nb, hist, ntiles, status);
         uint32_t* t;
         t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
         shift += nb;
     }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    if (ki != keys) {
-        e = cudaMemcpyAsync(keys, ki, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st);
-        if (e != cudaSuccess) return e;
-        e = cudaMemcpyAsync(vals, vi, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st);
-    }
-    return e;
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ cell ranges
@@ -387,10 +432,11 @@ __device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* 
 // Same arithmetic, order and caps.  The list is written in sorted-slot order (column
 // t - slot_base of the domain's block), so a warp's stores of entry k are consecutive
 // words; the collision pass reads the lists in the same order.  (Measured alternatives:
-// threads in object order, a warp per object, a warp per cell group, and (start, end)
-// pairs loaded three buckets at a time all ran slower — the walk is bound by load
-// latency, and sorted order with the highest occupancy gives the most shared bucket
-// reads.)
+// threads in object order, a warp per object, a warp per cell group, (start, end) pairs
+// loaded three buckets at a time, and the next bucket's range loaded ahead with
+// candidates loaded two or four at a time all ran slower — the walk is bound by load
+// latency, and this form's 32 registers give the highest occupancy and the most shared
+// bucket reads.)
 __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint2* __restrict__ cells,
                                                        const float4* __restrict__ ps,
                                                        const float4* __restrict__ x0s,
@@ -567,24 +613,26 @@ cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pi
     cudaError_t e = cudaMemsetAsync(d.cells, 0xff, sizeof(uint2) * (size_t)sentinel, st);
     if (e != cudaSuccess) return e;
     const int blocks = (hw + kBlock - 1) / kBlock;
-    k_hash_keys_arena<<<blocks, kBlock, 0, st>>>(pdom, d.dom, d.p[pin], d.keys, d.vals, hw, sentinel);
-    e = radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot, hw, bits, st, d.status);
+    const bool odd = radix_passes(hw, bits) % 2;
+    k_hash_keys_arena<<<blocks, kBlock, 0, st>>>(pdom, d.dom, d.p[pin], odd ? d.keys_tmp : d.keys,
+                                                 odd ? d.vals_tmp : d.vals, hw, sentinel);
+    e = radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, hw, bits, st, d.status);
     if (e != cudaSuccess) return e;
     k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, d.vals, pdom, d.p[pin], d.x0, hw, sentinel,
                                                    d.cells, d.ps, d.x0s, d.dslot);
     if (n_active > 0)
         k_cache_neighbors_arena<<<(n_active + kBlock - 1) / kBlock, kBlock, 0, st>>>(
             pdom, d.dom, d.cells, d.ps, d.x0s, d.nbr, d.dslot, n_active, d.status);
-    const int passes = (hw > 1 && bits > 0) ? (bits + 7) / 8 : 0;
-    if (launches) *launches += 3 + 3 * (uint64_t)passes;
+    if (launches) *launches += 3 + (uint64_t)radix_launches(hw, bits);
     return cudaGetLastError();
 }
 
-cudaError_t launch_hash_keys(const Launch& L, int pin)
+cudaError_t launch_hash_keys(const Launch& L, int pin, bool to_tmp)
 {
     if (!L.n_ptiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
-    k_hash_keys<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.p[pin], d.keys, d.vals);
+    k_hash_keys<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.p[pin], to_tmp ? d.keys_tmp : d.keys,
+                                                 to_tmp ? d.vals_tmp : d.vals);
     return cudaGetLastError();
 }
 
@@ -603,17 +651,18 @@ cudaError_t launch_cache_neighbors(const Launch& L, int pin)
 cudaError_t hash_objects_f3(uint32_t* phash, uint32_t* pindex, uint32_t* cell_start,
                             uint32_t* cell_end, uint32_t* neighbors, const float* positions,
                             const float* original, const vt_hash_params& hp,
-                            uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* hist,
-                            uint32_t* digit_tot, cudaStream_t st)
+                            uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* hist, cudaStream_t st)
 {
     const int32_t n = (int32_t)hp.num_objects;
     cudaError_t e = cudaMemsetAsync(cell_start, 0xff, sizeof(uint32_t) * ((size_t)hp.table_size + 1), st);
     if (e != cudaSuccess || n == 0) return e;
     const int blocks = (n + kBlock - 1) / kBlock;
-    k_hash_keys_f3<<<blocks, kBlock, 0, st>>>(positions, n, hp.cell_spacing, hp.table_size, phash, pindex);
     int bits = 0;
     while ((1ll << bits) < (long long)hp.table_size) ++bits;  // ceil(log2(tableSize))
-    e = radix_sort_pairs(phash, pindex, keys_tmp, vals_tmp, hist, digit_tot, n, bits, st);
+    const bool odd = radix_passes(n, bits) % 2;  // the sort reads the temporaries then
+    k_hash_keys_f3<<<blocks, kBlock, 0, st>>>(positions, n, hp.cell_spacing, hp.table_size,
+                                              odd ? keys_tmp : phash, odd ? vals_tmp : pindex);
+    e = radix_sort_pairs(phash, pindex, keys_tmp, vals_tmp, hist, n, bits, st);
     if (e != cudaSuccess) return e;
     k_cell_ranges<<<blocks, kBlock, 0, st>>>(phash, n, cell_start, cell_end);
     const uint64_t magic = ~0ull / (uint64_t)hp.table_size + 1ull;

@@ -10,7 +10,7 @@
 // in a fixed array compiled into this library instead.
 //
 // The array below is a file-scope __device__ variable of VT_HASH_NOALLOC_MAX_OBJECTS
-// objects' worth of scratch (about 2.2 MB).  Every GPU on which the library is loaded
+// objects' worth of scratch (about 2.4 MB).  Every GPU on which the library is loaded
 // holds it until the process exits.  In host code its name is only a host-side stand-in
 // for the device variable, never a device address: the address is obtained once per
 // device with cudaGetSymbolAddress and passed to the kernels.  The address is kept for
@@ -24,10 +24,8 @@
 namespace {
 
 constexpr int32_t kMaxObjects = VT_HASH_NOALLOC_MAX_OBJECTS;
-constexpr int32_t kTileItems = 4096;  // pairs per radix-sort tile (vt_hash.cu)
-// keys_tmp + vals_tmp + per-tile digit histograms + digit totals
-constexpr size_t kScratchWords = 2 * (size_t)kMaxObjects +
-                                 ((size_t)(kMaxObjects + kTileItems - 1) / kTileItems) * 256 + 256 + 256;
+// keys_tmp + vals_tmp + the sort's counts and look-back words
+constexpr size_t kScratchWords = 2 * (size_t)kMaxObjects + vt::radix_hist_words(kMaxObjects);
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kScratchWords];
 
@@ -87,17 +85,17 @@ static vt_status hash_objects_noalloc(uint32_t* particle_hash, uint32_t* particl
     uint32_t* keys_tmp = scratch;
     uint32_t* vals_tmp = keys_tmp + cap;
     uint32_t* hist = vals_tmp + cap;
-    uint32_t* digit_tot = hist + vt::radix_hist_words(n);
-    // the sort's layout must fit the fixed array (its tile size lives in vt_hash.cu)
-    if (2 * cap + vt::radix_hist_words(n) + 256 > kScratchWords) {
+    // the sort's layout must fit the fixed array
+    if (2 * cap + vt::radix_hist_words(n) > kScratchWords) {
         vt::set_error("vt_hash_objects_noalloc: the sort scratch for this table exceeds the fixed array");
         return VT_ERR_CAPACITY;
     }
-    // Nothing in the scratch has to start at zero: the sort writes every histogram, total
-    // and temporary key before reading it, so the previous call's contents are harmless.
+    // Nothing in the scratch has to start at zero: the sort clears its counts and
+    // look-back words on the stream before use and writes every temporary key before
+    // reading it, so the previous call's contents are harmless.
     cudaError_t e = vt::hash_objects_f3(particle_hash, particle_index, cell_start, cell_end, neighbors,
                                         positions, original_positions, *hp, keys_tmp, vals_tmp, hist,
-                                        digit_tot, (cudaStream_t)stream);
+                                        (cudaStream_t)stream);
     if (e != cudaSuccess) return vt::cuda_fail(e, "hash_objects (no-alloc)");
     return VT_OK;
 }

@@ -431,7 +431,7 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     // the arena
     auto tiles_bytes = [&](int64_t nt, size_t sz) { return ((nt * sz + 255) & ~size_t(255)); };
     const size_t a16 = ((size_t)cap * 16 + 255) & ~size_t(255), a4 = ((size_t)cap * 4 + 255) & ~size_t(255);
-    const size_t hist = (vt::radix_hist_words((int32_t)cap) * 4 + 255) & ~size_t(255);
+    const size_t hist = (vt::radix_hist_words(cap) * 4 + 255) & ~size_t(255);
     const size_t cells = ((size_t)cap * 3 * 4 + 255) & ~size_t(255), nbr = (size_t)cap * kMaxNbr * 4;
     const size_t small = M * (sizeof(vt::DomainParams) + kCollidersPerCloth * sizeof(vt::ColliderDev) +
                               2 * 16 * kSlotsPerCloth) + 4 * (M + 1) + 4 * M + 4096 * 4 +
@@ -450,7 +450,7 @@ vt_status vt_server_create(const vt_server_config* cfg, vt_server** out)
     s->pdom = (int32_t*)take(a4);
     s->d.keys = (uint32_t*)take(a4); s->d.vals = (uint32_t*)take(a4);
     s->d.keys_tmp = (uint32_t*)take(a4); s->d.vals_tmp = (uint32_t*)take(a4);
-    s->d.hist = (uint32_t*)take(hist); s->d.digit_tot = (uint32_t*)take(256 * 4);
+    s->d.hist = (uint32_t*)take(hist);
     s->d.cells = (uint2*)take(2 * cells);
     s->d.nbr = (uint32_t*)take(nbr);
     s->d.packed = (float*)take(a12);

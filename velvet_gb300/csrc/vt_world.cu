@@ -696,7 +696,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_tri = A.take<uint4>(TR), o_tno = A.take<int32_t>(N + 1), o_tne = A.take<int32_t>(tn.ent.size());
     const size_t o_k = A.take<uint32_t>(N), o_vl = A.take<uint32_t>(N);
     const size_t o_kt = A.take<uint32_t>(N), o_vt = A.take<uint32_t>(N);
-    const size_t o_h = A.take<uint32_t>(radix_hist_words((int32_t)N)), o_dt = A.take<uint32_t>(256);
+    const size_t o_h = A.take<uint32_t>(radix_hist_words(N));
     const size_t o_cs = A.take<uint2>(TK), o_nb = A.take<uint32_t>(NW);
     const size_t o_dom = A.take<DomainParams>(n_domains), o_col = A.take<ColliderDev>(C);
     const size_t o_pt = A.take<Tile>(pt.size()), o_bt = A.take<Tile>(bt.size());
@@ -722,7 +722,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     d.tri = AT(uint4, o_tri); d.tn_off = AT(int32_t, o_tno); d.tn_ent = AT(int32_t, o_tne);
     d.keys = AT(uint32_t, o_k); d.vals = AT(uint32_t, o_vl);
     d.keys_tmp = AT(uint32_t, o_kt); d.vals_tmp = AT(uint32_t, o_vt);
-    d.hist = AT(uint32_t, o_h); d.digit_tot = AT(uint32_t, o_dt);
+    d.hist = AT(uint32_t, o_h);
     d.cells = AT(uint2, o_cs); d.nbr = AT(uint32_t, o_nb);
     d.dom = AT(DomainParams, o_dom); d.col = AT(ColliderDev, o_col);
     d.ptiles = AT(Tile, o_pt); d.btiles = AT(Tile, o_bt); d.status = AT(int32_t, o_st);
@@ -873,9 +873,9 @@ int64_t World::launches_per_frame(int32_t S, int32_t It, int32_t ih, bool self, 
     int64_t L = 1 + 1;  // presdf_predict + normals
     int bits = 0;
     while ((1ll << bits) < (int64_t)tk) ++bits;
-    const int passes = (n > 1 && bits > 0) ? (bits + 7) / 8 : 0;
+    const int sort = radix_launches(n, bits);
     for (int s = 0; s < S; ++s) {
-        if (self && s % ih == 0) L += 3 + 3 * passes;  // keys, ranges, cache + sort
+        if (self && s % ih == 0) L += 3 + sort;  // keys, ranges, cache + sort
         L += 1;                                         // collide
         L += (int64_t)It * (bends ? 2 : 1);
         if (It == 0) L += 1;
@@ -962,7 +962,7 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
     int pc = 0;
     int bits = 0;
     while ((1ll << bits) < (int64_t)total_keys) ++bits;
-    const int sort_passes = (n_particles > 1 && bits > 0) ? (bits + 7) / 8 : 0;
+    const bool sort_odd = radix_passes(n_particles, bits) % 2;  // keys go to the temporaries
     const uint64_t pk = n_ptiles ? 1 : 0, bk = n_btiles ? 1 : 0;
 #define VT_STAGE(stage, call, what, count)          \
     do {                                            \
@@ -974,11 +974,11 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
     for (int sub = 0; sub < a.substeps; ++sub) {
         if (any_self && sub % ih == 0) {
             VT_CUDA(cudaMemsetAsync(d.cells, 0xff, (size_t)total_keys * sizeof(uint2), st), "memset cells");
-            VT_STAGE(ST_HASH_KEYS, launch_hash_keys(L, pc), "hash_keys", pk);
+            VT_STAGE(ST_HASH_KEYS, launch_hash_keys(L, pc, sort_odd), "hash_keys", pk);
             VT_STAGE(ST_RADIX_SORT,
-                     radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, d.digit_tot,
-                                      n_particles, bits, st, d.status),
-                     "radix_sort", 3 * (uint64_t)sort_passes);
+                     radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, n_particles,
+                                      bits, st, d.status),
+                     "radix_sort", (uint64_t)radix_launches(n_particles, bits));
             VT_STAGE(ST_CELL_RANGES, launch_cell_ranges_gather(d, pc, n_particles, st), "cell_ranges", 1);
             VT_STAGE(ST_CACHE_NEIGHBORS, launch_cache_neighbors(L, pc), "cache_neighbors", pk);
         }

@@ -194,7 +194,7 @@ struct DeviceArrays {
     float4 *grest = nullptr, *glra = nullptr;
     // hash
     uint32_t *keys = nullptr, *vals = nullptr, *keys_tmp = nullptr, *vals_tmp = nullptr;
-    uint32_t *hist = nullptr, *digit_tot = nullptr;
+    uint32_t* hist = nullptr;  // radix-sort scratch, radix_hist_words(n) words
     // cell ranges of the solver's hash: cells[h] = (start, end) of bucket h, start
     // 0xffffffff when empty, so one 8-byte load answers a bucket probe
     uint2* cells = nullptr;
@@ -284,13 +284,27 @@ cudaError_t launch_normals(const Launch& L);
 enum { SOLVE_PLAIN = 0, SOLVE_FINALIZE = 1, SOLVE_FINALIZE_PREDICT = 2 };
 
 // Spatial hash (vt_hash.cu)
-cudaError_t launch_hash_keys(const Launch& L, int pin);
-// Stable LSD radix sort of (keys, vals) pairs by the low `bits` bits of the keys;
-// result lands in keys / vals.  Scratch: keys_tmp, vals_tmp, hist, digit_tot.
+// Keys of the solver's particles into (keys, vals), or into (keys_tmp, vals_tmp) when
+// to_tmp (an odd number of sort passes; see radix_sort_pairs).
+cudaError_t launch_hash_keys(const Launch& L, int pin, bool to_tmp);
+// Stable LSD radix sort of (key, val) pairs by the low `bits` bits of the keys, in
+// radix_passes(n, bits) passes of up to 8 bits that move the pairs between (keys, vals)
+// and (keys_tmp, vals_tmp).  The input is read from keys / vals when the number of passes
+// is even and from keys_tmp / vals_tmp when it is odd; the result always lands in
+// keys / vals.  Scratch: hist, radix_hist_words(n) words, needing no initial contents.
+// radix_launches(n, bits) kernels are launched.
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
-                             uint32_t* vals_tmp, uint32_t* hist, uint32_t* digit_tot,
-                             int32_t n, int32_t bits, cudaStream_t st, int32_t* status = nullptr);
-size_t radix_hist_words(int32_t n);  // size of `hist` for n items
+                             uint32_t* vals_tmp, uint32_t* hist, int32_t n, int32_t bits,
+                             cudaStream_t st, int32_t* status = nullptr);
+int radix_passes(int32_t n, int32_t bits);
+int radix_launches(int32_t n, int32_t bits);
+constexpr int32_t kRadixTileItems = 4096;  // pairs per sort tile
+constexpr size_t kRadixScratchHead = 1280;  // digit counts and tile counters of 4 passes
+// size of `hist` for n items: the head plus a look-back word per (pass, tile, digit)
+constexpr size_t radix_hist_words(int64_t n)
+{
+    return kRadixScratchHead + (size_t)4 * 256 * (size_t)(n > kRadixTileItems ? (n + kRadixTileItems - 1) / kRadixTileItems : 1);
+}
 cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_start,
                                uint32_t* cell_end, cudaStream_t st);
 cudaError_t launch_cache_neighbors(const Launch& L, int pin);
@@ -300,12 +314,10 @@ cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pi
                               int32_t n_active, uint32_t sentinel, int32_t bits, cudaStream_t st,
                               uint64_t* launches);
 // HashObjects on float3 caller buffers (vt_hash_objects); scratch supplied by the caller:
-// keys_tmp / vals_tmp num_objects words each, hist radix_hist_words(num_objects),
-// digit_tot 256 words.
+// keys_tmp / vals_tmp num_objects words each, hist radix_hist_words(num_objects).
 cudaError_t hash_objects_f3(uint32_t* phash, uint32_t* pindex, uint32_t* cell_start,
                             uint32_t* cell_end, uint32_t* neighbors, const float* positions,
                             const float* original, const vt_hash_params& hp,
-                            uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* hist,
-                            uint32_t* digit_tot, cudaStream_t st);
+                            uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* hist, cudaStream_t st);
 
 }  // namespace vt
