@@ -509,20 +509,22 @@ struct PosF3 {
     }
 };
 
+// One block per particle tile (one domain).  The domain's sorted slots start at its first
+// particle's index in the world form and at dslot[domain] in the served form's arena.
 __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
-                  const uint2* __restrict__ cells, const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
-                  int32_t* __restrict__ status)
+                  const uint2* __restrict__ cells, const float4* __restrict__ ps, const float4* __restrict__ x0s,
+                  uint32_t* __restrict__ nbr, const int32_t* __restrict__ dslot, int32_t* __restrict__ status)
 {
     const Tile tl = tiles[blockIdx.x];
     const int t = tl.begin + (int)threadIdx.x;
     if (t >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
-    // a domain's sorted slots are its particle range
-    cache_neighbors_sorted((uint32_t)t, cells, ps, x0s, nbr + nbr_offset(D), (uint32_t)D.p_begin,
-                           (uint32_t)D.p_begin, D.p_count, D.table_base, D.table_size,
+    const uint32_t sbase = dslot ? (uint32_t)dslot[tl.dom] : (uint32_t)D.p_begin;
+    cache_neighbors_sorted(sbase + (uint32_t)(t - D.p_begin), cells, ps, x0s, nbr + nbr_offset(D),
+                           (uint32_t)D.p_begin, sbase, D.p_count, D.table_base, D.table_size,
                            ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2, D.diameter2,
-                           D.max_nbr, (uint32_t)(D.p_begin + D.p_count), status);
+                           D.max_nbr, sbase + (uint32_t)D.p_count, status);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -589,26 +591,11 @@ k_cell_ranges_arena(const uint32_t* __restrict__ keys, const uint32_t* __restric
     x0s[t] = x0[id];
 }
 
-__global__ void __launch_bounds__(kBlock)
-k_cache_neighbors_arena(const int32_t* __restrict__ pdom, const DomainParams* __restrict__ doms,
-                        const uint2* __restrict__ cells,
-                        const float4* __restrict__ ps, const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
-                        const int32_t* __restrict__ dslot, int32_t n_active, int32_t* __restrict__ status)
+cudaError_t launch_hash_arena(const Launch& L, const int32_t* pdom, int pin, int32_t hw,
+                              int32_t n_active, uint32_t sentinel, int32_t bits, uint64_t* launches)
 {
-    const int t = blockIdx.x * kBlock + (int)threadIdx.x;
-    if (t >= n_active) return;
-    const int32_t dom = pdom[__float_as_uint(ps[t].w)];
-    const DomainParams& D = doms[dom];
-    cache_neighbors_sorted((uint32_t)t, cells, ps, x0s, nbr + nbr_offset(D), (uint32_t)D.p_begin,
-                           (uint32_t)dslot[dom], D.p_count, D.table_base, D.table_size,
-                           ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, D.cell_spacing, D.cell_spacing2, D.diameter2,
-                           D.max_nbr, (uint32_t)n_active, status);
-}
-
-cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pin, int32_t hw,
-                              int32_t n_active, uint32_t sentinel, int32_t bits, cudaStream_t st,
-                              uint64_t* launches)
-{
+    const DeviceArrays& d = *L.d;
+    const cudaStream_t st = L.st;
     if (hw <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d.cells, 0xff, sizeof(uint2) * (size_t)sentinel, st);
     if (e != cudaSuccess) return e;
@@ -620,9 +607,10 @@ cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pi
     if (e != cudaSuccess) return e;
     k_cell_ranges_arena<<<blocks, kBlock, 0, st>>>(d.keys, d.vals, pdom, d.p[pin], d.x0, hw, sentinel,
                                                    d.cells, d.ps, d.x0s, d.dslot);
-    if (n_active > 0)
-        k_cache_neighbors_arena<<<(n_active + kBlock - 1) / kBlock, kBlock, 0, st>>>(
-            pdom, d.dom, d.cells, d.ps, d.x0s, d.nbr, d.dslot, n_active, d.status);
+    // the walk by particle tiles, each a block of one request's particles
+    if (n_active > 0 && L.n_ptiles)
+        k_cache_neighbors<<<L.n_ptiles, kBlock, 0, st>>>(d.ptiles, d.dom, d.cells, d.ps, d.x0s, d.nbr, d.dslot,
+                                                         d.status);
     if (launches) *launches += 3 + (uint64_t)radix_launches(hw, bits);
     return cudaGetLastError();
 }
@@ -642,7 +630,7 @@ cudaError_t launch_cache_neighbors(const Launch& L, int pin)
     const DeviceArrays& d = *L.d;
     (void)pin;  // positions come sorted from launch_cell_ranges_gather
     k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.cells, d.ps,
-                                                       d.x0s, d.nbr, d.status);
+                                                       d.x0s, d.nbr, nullptr, d.status);
     return cudaGetLastError();
 }
 

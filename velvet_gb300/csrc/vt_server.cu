@@ -364,8 +364,8 @@ vt_status run_frame(vt_server* s, cudaStream_t st)
     s->launches += 1;
     for (int sub = 0; sub < c.substeps; ++sub) {
         if (sub % s->interleaved_hash == 0)
-            VT_TRY_CUDA(vt::launch_hash_arena(s->d, s->pdom, pc, (int32_t)hw, (int32_t)s->active_particles,
-                                              sentinel, bits, st, &s->launches),
+            VT_TRY_CUDA(vt::launch_hash_arena(L, s->pdom, pc, (int32_t)hw, (int32_t)s->active_particles,
+                                              sentinel, bits, &s->launches),
                         "hash");
         VT_TRY_CUDA(vt::launch_collide(L, pc, 1 - pc), "collide");
         s->launches += 1;

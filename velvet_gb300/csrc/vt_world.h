@@ -310,9 +310,8 @@ cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_s
 cudaError_t launch_cache_neighbors(const Launch& L, int pin);
 // Spatial hash of a sparse particle arena (the served form): particles [0, hw) with
 // per-particle domain ids pdom (< 0: free); cells [0, sentinel); n_active live particles.
-cudaError_t launch_hash_arena(const DeviceArrays& d, const int32_t* pdom, int pin, int32_t hw,
-                              int32_t n_active, uint32_t sentinel, int32_t bits, cudaStream_t st,
-                              uint64_t* launches);
+cudaError_t launch_hash_arena(const Launch& L, const int32_t* pdom, int pin, int32_t hw,
+                              int32_t n_active, uint32_t sentinel, int32_t bits, uint64_t* launches);
 // HashObjects on float3 caller buffers (vt_hash_objects); scratch supplied by the caller:
 // keys_tmp / vals_tmp num_objects words each, hist radix_hist_words(num_objects).
 cudaError_t hash_objects_f3(uint32_t* phash, uint32_t* pindex, uint32_t* cell_start,
