@@ -789,8 +789,10 @@ def main() -> None:
                     help="frames per request when the served form runs the mixed-size workload")
     ap.add_argument("--tile-loads", choices=["tma", "cp_async"], default="cp_async",
                     help="how the grid kernel stages its tiles (same results)")
-    ap.add_argument("--substep-clusters", choices=["on", "off"], default="on",
-                    help="small grid cloths: a substep's iterations as one launch of thread-block clusters")
+    ap.add_argument("--substep-clusters", choices=["on", "restaging", "off"], default="on",
+                    help="small grid cloths: a substep's iterations as one launch of thread-block clusters "
+                         "(on: positions resident in shared memory where cloths fit 64x64; restaging: "
+                         "tiles re-read from global memory each iteration)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs")
     ap.add_argument("--no-exact-build", action="store_true",
                     help="skip timing the exact build beside the fast one")
@@ -810,10 +812,11 @@ def main() -> None:
         import velvet_gb300 as vg
 
         vg._abi.check(vg.lib().vt_tuning_set_tile_loads(1), "vt_tuning_set_tile_loads")
-    if args.substep_clusters == "off":
+    if args.substep_clusters != "on":
         import velvet_gb300 as vg
 
-        vg._abi.check(vg.lib().vt_tuning_set_substep_clusters(0), "vt_tuning_set_substep_clusters")
+        mode = {"off": 0, "restaging": 2}[args.substep_clusters]
+        vg._abi.check(vg.lib().vt_tuning_set_substep_clusters(mode), "vt_tuning_set_substep_clusters")
     if args.profile_frames:
         profile_frames(args)
         return

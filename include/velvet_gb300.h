@@ -478,14 +478,19 @@ vt_status vt_tuning_set_grid_tile(int32_t variant);
  * way; applies to frames enqueued (and CUDA graphs captured) afterwards.  No counterpart
  * in the reference (its kernels read global memory directly). */
 vt_status vt_tuning_set_tile_loads(int32_t tma);
-/* Small grid cloths (every cloth of a solver or batch within 16 tiles of the grid kernel)
- * run all Jacobi iterations of a substep in one launch: a thread-block cluster of 16
- * blocks per cloth steps through its tiles and separates the iterations with the
- * cluster's hardware barrier (on = 1, the default), instead of one launch per iteration
- * (0).  Same results; applies to frames enqueued, and CUDA graphs captured, afterwards (a
- * solver or batch that already captured its frame graph keeps it).  The reference
- * launches each constraint kernel once per iteration (Velvet/VtClothSolverGPU.hpp:90-96). */
-vt_status vt_tuning_set_substep_clusters(int32_t on);
+/* Small grid cloths run all Jacobi iterations of a substep in one launch of thread-block
+ * clusters, one cluster of 16 blocks per cloth, with the cluster's hardware barrier
+ * between iterations.  mode 1 (the default): when every cloth of a solver or batch is
+ * within 64 x 64 particles, each block keeps one 16 x 16 tile of predicted positions in
+ * shared memory for the whole substep and passes its edges to the neighbouring blocks
+ * through distributed shared memory; otherwise, when every cloth is within 16 tiles of
+ * the grid kernel, the blocks step through those tiles, reading positions from global
+ * memory each iteration.  mode 2: the latter form only.  mode 0: one launch per
+ * iteration.  Same results in every mode; applies to frames enqueued, and CUDA graphs
+ * captured, afterwards (a solver or batch that already captured its frame graph keeps
+ * it).  VT_ERR_INVALID_ARGUMENT for another mode.  The reference launches each constraint
+ * kernel once per iteration (Velvet/VtClothSolverGPU.hpp:90-96). */
+vt_status vt_tuning_set_substep_clusters(int32_t mode);
 /* The shape in use by a solver / batch (after its first frame). */
 vt_status vt_solver_grid_tile(const vt_solver* s, int32_t* variant);
 vt_status vt_batch_grid_tile(const vt_batch* b, int32_t* variant);

@@ -156,19 +156,25 @@ def test_tile_loads_by_tma_and_by_cp_async_give_the_oracle_bits(variant, tma):
         vg.lib().vt_tuning_set_tile_loads(0)
 
 
-@pytest.mark.parametrize("clusters", [1, 0], ids=["clusters", "per_iteration"])
+@pytest.mark.parametrize("clusters", [1, 2, 0], ids=["resident", "clusters", "per_iteration"])
 @pytest.mark.parametrize("variant", [0, 1, 2])
 def test_substeps_in_clusters_give_the_oracle_bits(variant, clusters):
     """Small grid cloths run a substep's iterations as one launch of 16-block clusters,
-    one per cloth, with the cluster barrier between iterations (or one launch per
-    iteration): the oracle's bits either way — a 40x40 cloth (9 to 14 tiles, one per block,
-    for the three shapes), a 24x24 one (fewer tiles than blocks), odd and even iteration counts,
-    the finalizing iterations between substeps, and a batch of small cloths."""
+    one per cloth, with the cluster barrier between iterations: positions resident in the
+    blocks' shared memory with halos passed through distributed shared memory (mode 1),
+    or re-read from global memory each iteration (mode 2), or one launch per iteration
+    (mode 0).  The oracle's bits in every mode: a 40x40 cloth (9 to 14 tiles, one per
+    block, for the three shapes; 3x3 resident tiles with partial edges), a 24x24 one
+    (fewer tiles than blocks), a 64x64 one (4x4 full resident tiles; two rounds of tiles in
+    mode 2 are not taken, so per-iteration launches), a 17x17 one with its whole top row
+    attached (more slots than the tile caches: the slot-group boxes), odd and even
+    iteration counts, the finalizing iterations between substeps, and a batch of small
+    cloths."""
     assert vg.lib().vt_tuning_set_substep_clusters(clusters) == 0
     assert vg.lib().vt_tuning_set_grid_tile(variant) == 0
     try:
-        for side, its in ((40, 10), (24, 3)):
-            spec = spec_of(side, 0.45)
+        for side, its, attached in ((40, 10, None), (24, 3, None), (64, 10, None), (17, 4, list(range(17)))):
+            spec = spec_of(side, 0.45, attached=attached)
             o, g = Oracle(), vg.ClothSolver()
             for s in (o, g):
                 W.build_plain(spec, s)
@@ -198,13 +204,19 @@ def test_substeps_in_clusters_give_the_oracle_bits(variant, clusters):
         vg.lib().vt_tuning_set_substep_clusters(1)
 
 
+def test_substep_cluster_mode_out_of_range_is_refused():
+    assert vg.lib().vt_tuning_set_substep_clusters(3) != 0
+    assert vg.lib().vt_tuning_set_substep_clusters(-1) != 0
+    assert vg.lib().vt_tuning_set_substep_clusters(1) == 0
+
+
 def test_substeps_in_clusters_cut_the_launches_of_a_small_cloth():
     """With clusters, a 32x32 cloth's frame launches one grid kernel per substep instead of
     one per iteration."""
     import ctypes as C
 
     counts = {}
-    for clusters in (1, 0):
+    for clusters in (1, 2, 0):
         assert vg.lib().vt_tuning_set_substep_clusters(clusters) == 0
         try:
             spec = spec_of(32, 0.45)
@@ -220,6 +232,7 @@ def test_substeps_in_clusters_cut_the_launches_of_a_small_cloth():
         finally:
             vg.lib().vt_tuning_set_substep_clusters(1)
     assert counts[0] - counts[1] == 5 * (10 - 1), counts
+    assert counts[2] == counts[1], counts
 
 
 @pytest.mark.parametrize("variant", [-1, 1, 5])

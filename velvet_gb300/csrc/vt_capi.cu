@@ -851,7 +851,7 @@ vt_status vt_solver_use_grid_kernel(vt_solver* s, int32_t on)
 
 vt_status vt_tuning_set_grid_tile(int32_t variant) { return vt::tuning_force(variant); }
 vt_status vt_tuning_set_tile_loads(int32_t tma) { return vt::set_tile_loads_tma(tma != 0); }
-vt_status vt_tuning_set_substep_clusters(int32_t on) { return vt::set_substep_clusters(on != 0); }
+vt_status vt_tuning_set_substep_clusters(int32_t mode) { return vt::set_substep_clusters(mode); }
 
 vt_status vt_solver_grid_tile(const vt_solver* s, int32_t* variant)
 {

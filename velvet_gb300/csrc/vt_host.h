@@ -164,6 +164,10 @@ private:
     int2* cloth_tiles_dev_ = nullptr;
     int32_t n_cluster_cloths_ = 0;
     bool cluster_ok_ = false;
+    // the resident form (every cloth within kResidentMaxSide): per cloth (domain, 0)
+    int2* cloth_doms_dev_ = nullptr;
+    int32_t n_resident_cloths_ = 0;
+    bool resident_ok_ = false;
     vt_status update_cluster_plan();
     // frame graph
     cudaStream_t cap_ = nullptr;

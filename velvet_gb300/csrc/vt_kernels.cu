@@ -525,6 +525,17 @@ __device__ __forceinline__ bool lra_group_quiet(vec3 p, vec3 x0, const float4* b
     return qu < (ql * c2) * kBoundDown;
 }
 
+// ApplyDeltas (VtClothSolverGPU.cu:253-264): the particle moved by the relaxed mean of
+// its constraints' corrections.
+__device__ __forceinline__ vec3 jacobi_apply(const DomainParams& D, vec3 pi, vec3 acc, int cnt)
+{
+    if (cnt > 0) {
+        const float count = (float)cnt;
+        pi = pi + (acc / count) * D.relax;
+    }
+    return pi;
+}
+
 // ApplyDeltas (VtClothSolverGPU.cu:253-264) and, by mode, Finalize (:388-407) and the
 // next substep's PredictPositions (:42-53); writes x, v, p_out of particle i.  `xsrc`
 // holds x[i] (global memory, or a shared-memory copy staged by the caller).
@@ -534,10 +545,7 @@ __device__ __forceinline__ void apply_and_finalize(const DomainParams& D, int do
                                                    float4* __restrict__ pout, float4* __restrict__ x,
                                                    float4* __restrict__ v, int32_t* __restrict__ status)
 {
-    if (cnt > 0) {
-        const float count = (float)cnt;
-        pi = pi + (acc / count) * D.relax;
-    }
+    pi = jacobi_apply(D, pi, acc, cnt);
     if (kMode == SOLVE_PLAIN) {
         pout[i] = make_float4(pi.x, pi.y, pi.z, wi);
         return;
@@ -1055,6 +1063,158 @@ k_grid_substep_cluster(const GridTile* __restrict__ tiles, const int2* __restric
     }
 }
 
+// Cluster-resident substep of a small grid cloth (up to 64 x 64 particles): a cluster of
+// 16 blocks, one 16 x 16 tile each, keeps the cloth's predicted positions in shared
+// memory for all of a substep's iterations.  Each block holds its tile plus a
+// one-particle halo in two buffers (this iteration's and the next's); a particle's new
+// position goes to its own block's next buffer and, on a tile edge, into the halo of the
+// neighbouring blocks' next buffers through distributed shared memory; the cluster
+// barrier (release / acquire) between iterations publishes those stores.  Global memory
+// is read once per substep (positions, rests, attachments) and written once (the last
+// iteration's finalize).  Generators and particle sums are the tile kernel's functions
+// on the same values, so the results are its bits.  320 threads: 17 x 17 generators,
+// 16 x 16 particles.
+constexpr int kResT = 16;
+constexpr int kResThreads = 320;
+constexpr int kResHalo = kResT + 2, kResGen = kResT + 1;
+static_assert(kResGen * kResGen <= kResThreads && kResT * kResT <= kResThreads, "threads cover the tile");
+static_assert(kClusterCtas == 16, "a 4 x 4 grid of tiles");
+
+struct ResidentSmem {
+    float4 sp[2][kResHalo][kResHalo];           // positions: this iteration's, the next's
+    float4 sst[4][kResGen][kResGen];            // stretch results, per type
+    float4 sbd[4][kResGen][kResGen];            // bending corner corrections
+    float4 sgr[kResGen * kResGen];              // generators' stretch rests (whole substep)
+    float4 sgl[kResT * kResT];                  // LRA rests, or the slot groups' boxes
+    float4 sx[kResT * kResT];                   // positions at the substep's start
+    float4 sslot[kGridLraCached];
+    float4 ssup[4 * (kLraGroupsMax / kLraSuper)];
+    __align__(16) DomainParams sdom;
+};
+
+__device__ __forceinline__ void st_cluster_f4(const float4* local, uint32_t rank, float4 v)
+{
+    const uint32_t la = (uint32_t)__cvta_generic_to_shared(local);
+    uint32_t ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(la), "r"(rank));
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(ra), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(kResThreads, 1)
+k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* __restrict__ doms,
+                        float4* __restrict__ p0, float4* __restrict__ p1, float4* __restrict__ x,
+                        float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ grest,
+                        const float4* __restrict__ glra, const float4* __restrict__ slots,
+                        const float4* __restrict__ slots0, int32_t* __restrict__ status, int pin0,
+                        int iterations, int last_substep)
+{
+    extern __shared__ __align__(128) unsigned char res_smem[];
+    ResidentSmem& S = *reinterpret_cast<ResidentSmem*>(res_smem);
+    const int dom = cloth_dom[blockIdx.x / kClusterCtas].x;
+    const int rank = (int)(blockIdx.x % kClusterCtas);  // the block's rank in its 1-D cluster
+    const int tid = (int)threadIdx.x;
+    if (tid < (int)(sizeof(DomainParams) / 16))
+        cp_async16(reinterpret_cast<float4*>(&S.sdom) + tid, reinterpret_cast<const float4*>(doms + dom) + tid);
+    cp_async_wait_all();
+    __syncthreads();
+    const DomainParams& D = S.sdom;
+    const int R = D.grid_res, V = R + 1, base = D.p_begin;
+    const int rt = rank >> 2, rc = rank & 3;            // the block's tile in the 4 x 4 grid
+    const int a0 = kResT * rt, b0 = kResT * rc;
+    const bool active = a0 < V && b0 < V;
+    const int ns = D.grid_slot_count, s0 = D.grid_slot_begin;
+    const int gx = tid / kResGen, gy = tid - gx * kResGen;  // generator (a0 - 1 + gx, b0 - 1 + gy)
+    const bool has_gen = tid < kResGen * kResGen;
+    const int ta = tid / kResT, tb = tid - ta * kResT;     // particle (a0 + ta, b0 + tb)
+    const int a = a0 + ta, b = b0 + tb;
+    const int i = base + a * V + b;
+    // a thread never leaves before the end: every thread takes part in the cluster barriers
+    const bool owns = active && tid < kResT * kResT && a < V && b < V &&
+                      VT_IN_RANGE(i, D.p_begin, D.p_begin + D.p_count, status);
+    const float4* pin = pin0 ? p1 : p0;
+    const bool stage_lra = ns >= 1 && ns <= kGridLraCached;
+
+    // stage the tile and halo (zero outside the cloth; the next buffer's halo starts at
+    // zero and stays so outside the cloth), the rests, the attachments and x
+    if (active) {
+        for (int k = tid; k < kResHalo * kResHalo; k += kResThreads) {
+            const int ha = k / kResHalo, hb = k - ha * kResHalo;
+            const int pa = a0 - 1 + ha, pb = b0 - 1 + hb;
+            const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V;
+            cp_async16_zfill(&S.sp[0][ha][hb], pin + (in ? base + pa * V + pb : base), in);
+            S.sp[1][ha][hb] = make_float4(0, 0, 0, 0);
+        }
+        if (has_gen) {
+            const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
+            const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
+            cp_async16_zfill(&S.sgr[tid], grest + (gen ? base + X * V + Y : base), gen);
+        }
+        if (owns && stage_lra) cp_async16(&S.sgl[tid], glra + i);
+        if (owns) cp_async16(&S.sx[tid], x + i);
+        if (tid < ns && tid < kGridLraCached) cp_async16(&S.sslot[tid], slots + s0 + tid);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    int gsize = 0, ngroups = 0;
+    if (active && ns > kGridLraCached) {
+        gsize = max(kLraGroupMin, (ns + kLraGroupsMax - 1) / kLraGroupsMax);
+        ngroups = (ns + gsize - 1) / gsize;
+        lra_group_boxes(S.sgl, S.ssup, slots + s0, slots0 + s0, ns, gsize, ngroups, tid);
+    }
+    // every block's next buffer is cleared before any neighbour stores into it
+    cluster_barrier();
+
+    int pc = pin0;
+    for (int it = 0; it < iterations; ++it) {
+        const int cur = it & 1;
+        if (active && has_gen)
+            grid_generator<kResHalo, kResGen, kResGen>(a0 - 1 + gx, b0 - 1 + gy, R, S.sp[cur], gx, gy, S.sst,
+                                                       S.sbd, gx, gy, S.sgr[tid], D.xpbd_bend);
+        __syncthreads();
+        if (owns) {
+            const int hx = ta + 1, hy = tb + 1;
+            const float4 pi4 = S.sp[cur][hx][hy];
+            const vec3 pi = xyz(pi4);
+            const float wi = pi4.w;
+            vec3 acc = mk3(0, 0, 0);
+            int cnt = 0;
+            grid_particle_sum<kResGen, kResGen>(a, b, R, i, hx, hy, S.sst, S.sbd, pi, wi, ns, s0, &S.sgl[tid],
+                                                S.sslot, S.sgl, S.ssup, gsize, ngroups, x0, slots, slots0, D.lrs,
+                                                acc, cnt);
+            if (it + 1 < iterations) {
+                const vec3 np = jacobi_apply(D, pi, acc, cnt);
+                const float4 q = make_float4(np.x, np.y, np.z, wi);
+                const int nx = cur ^ 1;
+                S.sp[nx][hx][hy] = q;
+                // edge particles into the halos of the neighbouring tiles (which exist:
+                // the halo particle a0 - 1 etc. lies in the cloth)
+                const bool up = ta == 0 && rt > 0, down = ta == kResT - 1 && rt < 3;
+                const bool left = tb == 0 && rc > 0, right = tb == kResT - 1 && rc < 3;
+                if (up) st_cluster_f4(&S.sp[nx][kResT + 1][hy], (uint32_t)(rank - 4), q);
+                if (down) st_cluster_f4(&S.sp[nx][0][hy], (uint32_t)(rank + 4), q);
+                if (left) st_cluster_f4(&S.sp[nx][hx][kResT + 1], (uint32_t)(rank - 1), q);
+                if (right) st_cluster_f4(&S.sp[nx][hx][0], (uint32_t)(rank + 1), q);
+                if (up && left) st_cluster_f4(&S.sp[nx][kResT + 1][kResT + 1], (uint32_t)(rank - 5), q);
+                if (up && right) st_cluster_f4(&S.sp[nx][kResT + 1][0], (uint32_t)(rank - 3), q);
+                if (down && left) st_cluster_f4(&S.sp[nx][0][kResT + 1], (uint32_t)(rank + 3), q);
+                if (down && right) st_cluster_f4(&S.sp[nx][0][0], (uint32_t)(rank + 5), q);
+            } else {
+                float4* po = pc ? p0 : p1;  // this iteration's output buffer
+                if (last_substep)
+                    apply_and_finalize<SOLVE_FINALIZE>(D, dom, i, pi, wi, acc, cnt, &S.sx[tid], po, x, v, status);
+                else
+                    apply_and_finalize<SOLVE_FINALIZE_PREDICT>(D, dom, i, pi, wi, acc, cnt, &S.sx[tid], po, x, v,
+                                                               status);
+            }
+        }
+        // publishes the halo stores; no block reads this iteration's buffers afterwards
+        cluster_barrier();
+        pc ^= 1;
+    }
+}
+
 template <int kPredict>
 __global__ void __launch_bounds__(kBlock)
 k_finalize(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
@@ -1339,6 +1499,55 @@ bool substep_clusters_supported()
     static int ok = -1;
     if (ok < 0) {
         ok = cluster_kernel_fits<7, 31>() && cluster_kernel_fits<15, 15>() && cluster_kernel_fits<3, 63>() ? 1 : 0;
+        (void)cudaGetLastError();  // a refused query leaves no sticky error
+    }
+    return ok == 1;
+}
+
+static cudaLaunchConfig_t resident_config(const Launch& L, int n_cloths, cudaLaunchAttribute* at)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(kClusterCtas * n_cloths));
+    cfg.blockDim = dim3(kResThreads);
+    cfg.dynamicSmemBytes = sizeof(ResidentSmem);
+    cfg.stream = L.st;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kClusterCtas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom, int n_cloths, int pin,
+                                         int iterations, int last_sub)
+{
+    if (n_cloths <= 0 || iterations <= 0) return cudaSuccess;
+    const DeviceArrays& d = *L.d;
+    cudaLaunchAttribute at[1];
+    const cudaLaunchConfig_t cfg = resident_config(L, n_cloths, at);
+    return cudaLaunchKernelEx(&cfg, k_grid_substep_resident, cloth_dom, (const DomainParams*)d.dom, d.p[0], d.p[1],
+                              d.x, d.v, (const float4*)d.x0, (const float4*)d.grest, (const float4*)d.glra,
+                              (const float4*)d.slots, (const float4*)d.slots0, d.status, pin, iterations, last_sub);
+}
+
+bool substep_resident_supported()
+{
+    static int ok = -1;
+    if (ok < 0) {
+        auto k = k_grid_substep_resident;
+        bool fits = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+                    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(ResidentSmem)) == cudaSuccess;
+        if (fits) {
+            Launch L{};
+            cudaLaunchAttribute at[1];
+            const cudaLaunchConfig_t cfg = resident_config(L, 1, at);
+            int n = 0;
+            fits = cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n >= 1;
+        }
+        ok = fits ? 1 : 0;
         (void)cudaGetLastError();  // a refused query leaves no sticky error
     }
     return ok == 1;

@@ -254,12 +254,16 @@ bool encode_grid_tmaps(CUtensorMap* dst, const float4* p0, const float4* p1, con
 bool tile_loads_tma() { return g_tile_tma.load(); }
 
 namespace {
-std::atomic<bool> g_substep_clusters{true};
+std::atomic<int> g_substep_clusters{1};
 }
-bool substep_clusters_enabled() { return g_substep_clusters.load(); }
-vt_status set_substep_clusters(bool on)
+int substep_clusters_mode() { return g_substep_clusters.load(); }
+vt_status set_substep_clusters(int mode)
 {
-    g_substep_clusters.store(on);
+    if (mode < 0 || mode > 2) {
+        set_error("substep cluster mode must be 0, 1 or 2");
+        return VT_ERR_INVALID_ARGUMENT;
+    }
+    g_substep_clusters.store(mode);
     return VT_OK;
 }
 vt_status set_tile_loads_tma(bool on)
@@ -369,8 +373,26 @@ vt_status World::set_grid_variant(int variant)
 vt_status World::update_cluster_plan()
 {
     cluster_ok_ = false;
+    resident_ok_ = false;
     n_cluster_cloths_ = 0;
     if (grid_doms_.empty() || n_stiles || n_btiles || (int32_t)grid_doms_.size() != n_domains) return VT_OK;
+    {
+        // the resident form: every cloth within 4 x 4 tiles of 16 x 16 particles
+        std::vector<int2> doms;
+        for (auto& gd : grid_doms_) {
+            if (hdom[gd.first].grid_res + 1 > kResidentMaxSide) {
+                doms.clear();
+                break;
+            }
+            doms.push_back(make_int2(gd.first, 0));
+        }
+        if (!doms.empty() && substep_resident_supported()) {
+            VT_CUDA(cudaMemcpy(cloth_doms_dev_, doms.data(), doms.size() * sizeof(int2), cudaMemcpyHostToDevice),
+                    "upload resident cloth list");
+            n_resident_cloths_ = (int32_t)doms.size();
+            resident_ok_ = true;
+        }
+    }
     std::vector<int2> ranges;
     int32_t t0 = 0;
     for (auto& gd : grid_doms_) {
@@ -707,7 +729,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     const size_t o_st = A.take<int32_t>(1 + n_domains), o_pk = A.take<float>(3 * (size_t)N);
     const size_t o_ps = A.take<float4>(N), o_x0s = A.take<float4>(N);
     const size_t o_tm = A.take<CUtensorMap>(any_grid ? (size_t)kTmapsPerDomain * n_domains : 0);
-    const size_t o_ctl = A.take<int2>(n_domains);
+    const size_t o_ctl = A.take<int2>(n_domains), o_cdl = A.take<int2>(n_domains);
     bytes = A.off;
     VT_CUDA(cudaMalloc(&arena_, A.off), "cudaMalloc(world)");
     char* base = (char*)arena_;
@@ -731,6 +753,7 @@ vt_status World::build(const std::vector<const HostSolver*>& S)
     d.ps = AT(float4, o_ps); d.x0s = AT(float4, o_x0s);
     CUtensorMap* tmaps_dev = any_grid ? AT(CUtensorMap, o_tm) : nullptr;
     cloth_tiles_dev_ = AT(int2, o_ctl);
+    cloth_doms_dev_ = AT(int2, o_cdl);
 #undef AT
     auto up = [](void* dst, const void* src, size_t bytes_) -> cudaError_t {
         return bytes_ ? cudaMemcpy(dst, src, bytes_, cudaMemcpyHostToDevice) : cudaSuccess;
@@ -985,7 +1008,16 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
         VT_STAGE(ST_COLLIDE, launch_collide(L, pc, 1 - pc), "collide", pk);
         pc = 1 - pc;
         const bool last_sub = sub == a.substeps - 1;
-        if (cluster_ok_ && a.iterations > 0 && substep_clusters_enabled()) {
+        const int cmode = substep_clusters_mode();
+        if (resident_ok_ && a.iterations > 0 && cmode == 1) {
+            // small grid cloths: the substep's iterations in one launch, positions resident
+            // in the clusters' shared memory
+            VT_STAGE(ST_GRID_ITER,
+                     launch_grid_substep_resident(L, cloth_doms_dev_, n_resident_cloths_, pc, a.iterations,
+                                                  last_sub ? 1 : 0),
+                     "grid_iter", 1);
+            if (a.iterations % 2) pc = 1 - pc;
+        } else if (cluster_ok_ && a.iterations > 0 && cmode != 0) {
             // small grid cloths: the substep's iterations in one launch of clusters
             VT_STAGE(ST_GRID_ITER,
                      launch_grid_substep_cluster(L, cloth_tiles_dev_, n_cluster_cloths_, pc, a.iterations,

@@ -269,9 +269,17 @@ bool substep_clusters_supported();
 // tiles of 15x15 on 16 blocks — each iteration pays the tile's dependent-latency chain
 // twice and the frame took 0.62 ms against 0.48 ms with one launch per iteration.)
 constexpr int kClusterMaxTiles = 16;
-// Whether small-cloth worlds run a substep's iterations as one cluster launch (default).
-bool substep_clusters_enabled();
-vt_status set_substep_clusters(bool on);
+// How small-cloth worlds run a substep's iterations: 0 one launch per iteration; 1 (the
+// default) one launch of cluster-resident tiles when every cloth is within
+// kResidentMaxSide particles a side, else one launch of clusters stepping through the
+// tile kernel's tiles when every cloth is within kClusterMaxTiles tiles; 2 the latter
+// only.
+constexpr int kResidentMaxSide = 64;
+int substep_clusters_mode();
+vt_status set_substep_clusters(int mode);
+cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom, int n_cloths, int pin,
+                                         int iterations, int last_sub);
+bool substep_resident_supported();
 
 cudaError_t launch_presdf_predict(const Launch& L, int pcur);
 cudaError_t launch_collide(const Launch& L, int pin, int pout);
