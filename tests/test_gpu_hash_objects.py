@@ -88,13 +88,15 @@ def test_hash_objects_empty_and_single():
     _check(one, one, 0.05, 2, 64, 0.03)
 
 
+@pytest.mark.parametrize("n", [70_000, 4_000])
 @pytest.mark.parametrize("T", [200, 40_000, 300_000, (1 << 25) + 1])
-def test_hash_objects_sort_passes_one_to_four(T):
+def test_hash_objects_sort_passes_one_to_four(T, n):
     """Tables whose key widths (8, 16, 19 and 26 bits) make the radix sort run one, two,
     three and four digit passes: an odd count starts from the temporaries, and every
-    count must leave the sorted pairs in the caller's buffers."""
-    rng = np.random.default_rng(T)
-    n = 70_000  # 18 sort tiles, so each pass's look-back crosses tiles
+    count must leave the sorted pairs in the caller's buffers.  70,000 objects span 18
+    sort tiles, so each pass's look-back crosses tiles; 4,000 fit one tile, sorted by a
+    single block with the pairs in shared memory between passes."""
+    rng = np.random.default_rng(T + n)
     pos = rng.uniform(-1.0, 1.0, (n, 3)).astype(np.float32)
     pos[:, 1] *= 0.2
     orig = (pos + rng.normal(0.0, 0.05, (n, 3))).astype(np.float32)

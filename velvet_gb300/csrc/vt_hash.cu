@@ -111,7 +111,8 @@ int radix_passes(int32_t n, int32_t bits) { return (n > 1 && bits > 0) ? (bits +
 int radix_launches(int32_t n, int32_t bits)
 {
     const int passes = radix_passes(n, bits);
-    return passes ? 1 + passes : 0;
+    if (!passes) return 0;
+    return n <= kRadixTileItems ? 1 : 1 + passes;
 }
 
 __device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t* a)
@@ -285,6 +286,83 @@ k_rs_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin
     }
 }
 
+// All passes of a sort that fits one tile (n <= 4096) in one block: the pairs stay in
+// shared memory between passes, and each pass's digit offsets are the tile's own prefix
+// sums, so no count kernel, look-back or scratch is needed.  Same ranking as
+// k_rs_onesweep, so the same stable order.
+__global__ void __launch_bounds__(kBlock)
+k_rs_single_tile(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+                 uint32_t* __restrict__ vout, int32_t n, int passes, int per, int bits, int32_t* __restrict__ status)
+{
+    __shared__ uint32_t lofs[256];
+    __shared__ uint32_t wcnt[kRsWarps][256];
+    __shared__ uint32_t sk[kRsTile], sv[kRsTile];
+    for (int k = threadIdx.x; k < n; k += kBlock) {
+        sk[k] = kin[k];
+        sv[k] = vin[k];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    const int wbase = warp * (32 * kRsItems);
+    int shift = 0;
+    for (int ps = 0; ps < passes; ++ps) {
+        const int nb = min(per, bits - shift);
+        const int ndig = 1 << nb;
+        const uint32_t mask = (uint32_t)ndig - 1;
+        for (int k = threadIdx.x; k < kRsWarps * 256; k += kBlock) (&wcnt[0][0])[k] = 0;
+        __syncthreads();  // the pairs are in place and the counters cleared
+        uint32_t mk[kRsItems], mv[kRsItems], mr[kRsItems];
+#pragma unroll
+        for (int j = 0; j < kRsItems; ++j) {
+            const int idx = wbase + j * 32 + lane;
+            const bool valid = idx < n;
+            const uint32_t key = valid ? sk[idx] : 0u;
+            const uint32_t val = valid ? sv[idx] : 0u;
+            const uint32_t d = valid ? ((key >> shift) & mask) : 0x100u;  // 0x100: not a digit
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            uint32_t rank = 0;
+            if (valid) rank = wcnt[warp][d] + __popc(peers & lt);
+            __syncwarp();
+            if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] += __popc(peers);
+            __syncwarp();
+            mk[j] = key;
+            mv[j] = val;
+            mr[j] = rank;
+        }
+        __syncthreads();  // every pair is in registers and every warp has counted
+        uint32_t run = 0;
+        if ((int)threadIdx.x < ndig) {
+#pragma unroll
+            for (int w = 0; w < kRsWarps; ++w) {
+                const uint32_t c = wcnt[w][threadIdx.x];
+                wcnt[w][threadIdx.x] = run;
+                run += c;
+            }
+        }
+        uint32_t tot;
+        const uint32_t lex = block_exclusive_scan(run, &tot);
+        if ((int)threadIdx.x < ndig) lofs[threadIdx.x] = lex;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kRsItems; ++j) {
+            const int idx = wbase + j * 32 + lane;
+            if (idx < n) {
+                const uint32_t d = (mk[j] >> shift) & mask;
+                const uint32_t lp = lofs[d] + wcnt[warp][d] + mr[j];
+                if (!VT_IN_RANGE(lp, 0, n, status)) continue;
+                sk[lp] = mk[j];
+                sv[lp] = mv[j];
+            }
+        }
+        shift += nb;
+        __syncthreads();  // the pass's pairs are placed and its counters read
+    }
+    for (int k = threadIdx.x; k < n; k += kBlock) {
+        kout[k] = sk[k];
+        vout[k] = sv[k];
+    }
+}
+
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp, uint32_t* vals_tmp,
                              uint32_t* hist, int32_t n, int32_t bits, cudaStream_t st, int32_t* status)
 {
@@ -293,13 +371,17 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
     if (passes > kRsMaxPasses || n > (int32_t)kRsCountMask) return cudaErrorInvalidValue;
     const int per = (bits + passes - 1) / passes;
     const int32_t ntiles = (n + kRsTile - 1) / kRsTile;
-    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * (kRsLookBase + (size_t)passes * ntiles * 256), st);
-    if (e != cudaSuccess) return e;
     // an odd number of passes starts from the temporaries, so the result lands in keys / vals
     uint32_t *ki = keys, *vi = vals, *ko = keys_tmp, *vo = vals_tmp;
     if (passes % 2) {
         ki = keys_tmp; vi = vals_tmp; ko = keys; vo = vals;
     }
+    if (ntiles == 1) {
+        k_rs_single_tile<<<1, kBlock, 0, st>>>(ki, vi, keys, vals, n, passes, per, bits, status);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * (kRsLookBase + (size_t)passes * ntiles * 256), st);
+    if (e != cudaSuccess) return e;
     k_rs_count<<<ntiles < 1024 ? ntiles : 1024, kBlock, 0, st>>>(ki, n, passes, per, bits, hist);
     int shift = 0;
     for (int ps = 0; ps < passes; ++ps) {
@@ -527,6 +609,87 @@ k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict
                            D.max_nbr, sbase + (uint32_t)D.p_count, status);
 }
 
+// The same lists with a warp per particle, for worlds too small to hide the thread form's
+// serial chain of 27 bucket probes: lane q < 27 probes bucket q (q = 9a + 3b + c, the
+// walk's order) and tests its candidates, a warp prefix sum of the lanes' counts places
+// each bucket's entries after those of the buckets before it, and a second pass over the
+// candidates (now in L1) writes the entries that fall within the list's cap.  Same
+// tests, order and caps as cache_neighbors_sorted.  Each block serves eight particles of
+// one particle tile: block b takes tile b / 32 and its particles 8 (b % 32) .. + 7.
+__global__ void __launch_bounds__(kBlock)
+k_cache_neighbors_warp(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+                       const uint2* __restrict__ cells, const float4* __restrict__ ps,
+                       const float4* __restrict__ x0s, uint32_t* __restrict__ nbr,
+                       const int32_t* __restrict__ dslot, int32_t* __restrict__ status)
+{
+    const Tile tl = tiles[blockIdx.x >> 5];
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    const int t = tl.begin + (int)(blockIdx.x & 31) * 8 + warp;
+    if (t >= tl.end) return;  // the whole warp
+    const DomainParams& D = doms[tl.dom];
+    const uint32_t sbase = dslot ? (uint32_t)dslot[tl.dom] : (uint32_t)D.p_begin;
+    const uint32_t slot = sbase + (uint32_t)(t - D.p_begin);
+    const int32_t n = D.p_count;
+    const uint32_t slot_end = sbase + (uint32_t)n, id_base = (uint32_t)D.p_begin;
+    const float4 own = ps[slot];
+    const uint32_t id = __float_as_uint(own.w);
+    const vec3 position = xyz(own);
+    const float sp = D.cell_spacing;
+    const int32_t ix = int_coord(position.x, sp), iy = int_coord(position.y, sp), iz = int_coord(position.z, sp);
+    const int max_nbr = D.max_nbr;
+    uint32_t start = 0, end = 0;
+    if (lane < 27) {
+        const int a = lane / 9, b = (lane / 3) % 3, c = lane % 3;
+        const uint32_t key = ((uint32_t)(ix - 1 + a) * 92837111u) ^ ((uint32_t)(iy - 1 + b) * 689287499u) ^
+                             ((uint32_t)(iz - 1 + c) * 283923481u);
+        const uint32_t h = (uint32_t)D.table_base +
+                           abs_mod(key, ((uint64_t)D.tmod_hi << 32) | D.tmod_lo, (uint32_t)D.table_size);
+        const uint2 range = cells[h];
+        if (range.x != 0xffffffffu) {
+            uint32_t e = range.y;
+            const uint32_t lim = range.x + (uint32_t)max_nbr;
+            if (lim < e) e = lim;
+            if (VT_IN_RANGE(e, range.x, (long long)slot_end + 1, status)) {
+                start = range.x;
+                end = e;
+            }
+        }
+    }
+    const vec3 originalp = xyz(x0s[slot]);
+    const float sp2 = D.cell_spacing2, diam2 = D.diameter2;
+    auto fires = [&](uint32_t k, uint32_t& nb) {
+        const float4 qk = ps[k];
+        nb = __float_as_uint(qk.w);
+        if (!VT_IN_RANGE(nb, id_base, id_base + (uint32_t)n, status)) return false;
+        const vec3 d1 = position - xyz(qk);
+        if (nb == id) return false;
+        if (!(dot(d1, d1) < sp2)) return false;
+        const vec3 d2 = originalp - xyz(x0s[k]);
+        return dot(d2, d2) > diam2;
+    };
+    uint32_t cnt = 0;
+    for (uint32_t k = start; k < end; ++k) {
+        uint32_t nb;
+        if (fires(k, nb)) ++cnt;
+    }
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t* out = nbr + nbr_offset(D) + (slot - sbase);
+    uint32_t pos = incl - cnt;
+    if (cnt && pos < (uint32_t)max_nbr) {
+        for (uint32_t k = start; k < end && pos < (uint32_t)max_nbr; ++k) {
+            uint32_t nb;
+            if (fires(k, nb)) out[(size_t)(pos++) * n] = nb;
+        }
+    }
+    if (lane == 0 && total < (uint32_t)max_nbr) out[(size_t)total * n] = 0xffffffffu;
+}
+
 __global__ void __launch_bounds__(kBlock)
 k_cache_neighbors_f3(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ cs,
                      const uint32_t* __restrict__ ce, const float* __restrict__ pos,
@@ -629,8 +792,12 @@ cudaError_t launch_cache_neighbors(const Launch& L, int pin)
     if (!L.n_ptiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
     (void)pin;  // positions come sorted from launch_cell_ranges_gather
-    k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.cells, d.ps,
-                                                       d.x0s, d.nbr, nullptr, d.status);
+    if (L.n_particles <= kWarpWalkMaxParticles)
+        k_cache_neighbors_warp<<<L.n_ptiles * 32, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.cells, d.ps, d.x0s, d.nbr,
+                                                                     nullptr, d.status);
+    else
+        k_cache_neighbors<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.cells, d.ps, d.x0s, d.nbr, nullptr,
+                                                           d.status);
     return cudaGetLastError();
 }
 
