@@ -1081,6 +1081,14 @@ __device__ __forceinline__ void cluster_barrier()
 {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void cluster_arrive()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait()
+{
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 template <int kTA, int kTB>
 __global__ void __launch_bounds__(kBlock, 1)
@@ -1180,10 +1188,34 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
     const int a0 = kResT * rt, b0 = kResT * rc;
     const bool active = a0 < V && b0 < V;
     const int ns = D.grid_slot_count, s0 = D.grid_slot_begin;
+    // generators (a0 - 1 + gx, b0 - 1 + gy): the 15 x 15 interior ones (no halo position
+    // read) first, then the 64 on the border; warps whose generators are all interior
+    // compute before waiting for the neighbours' halo stores
     const bool bend_half = tid >= kResHalf;
     const int g = bend_half ? tid - kResHalf : tid;
-    const int gx = g / kResGen, gy = g - gx * kResGen;  // generator (a0 - 1 + gx, b0 - 1 + gy)
+    constexpr int kInner = (kResGen - 2) * (kResGen - 2);
+    int gx, gy;
+    if (g < kInner) {
+        gx = 1 + g / (kResGen - 2);
+        gy = 1 + g % (kResGen - 2);
+    } else {
+        const int e = g - kInner;  // row 0, row 16, column 0, column 16
+        if (e < kResGen) {
+            gx = 0;
+            gy = e;
+        } else if (e < 2 * kResGen) {
+            gx = kResGen - 1;
+            gy = e - kResGen;
+        } else if (e < 2 * kResGen + (kResGen - 2)) {
+            gx = 1 + e - 2 * kResGen;
+            gy = 0;
+        } else {
+            gx = 1 + e - 2 * kResGen - (kResGen - 2);
+            gy = kResGen - 1;
+        }
+    }
     const bool has_gen = g < kResGen * kResGen;
+    const bool inner_warp = ((tid >> 5) % (kResHalf / 32)) * 32 + 31 < kInner;
     const int ta = tid / kResT, tb = tid - ta * kResT;     // particle (a0 + ta, b0 + tb)
     const int a = a0 + ta, b = b0 + tb;
     const int i = base + a * V + b;
@@ -1226,6 +1258,9 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
     int pc = pin0;
     for (int it = 0; it < iterations; ++it) {
         const int cur = it & 1;
+        // the previous iteration's halo stores are published by the cluster barrier it
+        // arrived at; interior generators read only this block's positions
+        if (it > 0 && !inner_warp) cluster_wait();
         if (active && has_gen) {
             const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
             if (!bend_half) {
@@ -1239,6 +1274,7 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
                                                                 D.xpbd_bend);
             }
         }
+        if (it > 0 && inner_warp) cluster_wait();
         __syncthreads();
         if (owns) {
             const int hx = ta + 1, hy = tb + 1;
@@ -1276,8 +1312,10 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
                                                                status);
             }
         }
-        // publishes the halo stores; no block reads this iteration's buffers afterwards
-        cluster_barrier();
+        if (it + 1 < iterations) {
+            cluster_arrive();  // after this thread's halo stores (release)
+            __syncthreads();   // the sums have read sst / sbd and written this block's positions
+        }
         pc ^= 1;
     }
 }
