@@ -200,9 +200,6 @@ ColliderDev collider_to_device(const vt_sdf_collider& c);
 
 // Grid kernel variant to use: the forced one (vt_tuning_set), else `tuned`.
 int grid_variant_for(int tuned);
-// Last autotuned variant in this process (the default one if none), for worlds that do
-// not tune (the served form).
-int last_tuned_variant();
 // Forces a grid kernel variant for every world (-1: autotune again).
 vt_status tuning_force(int32_t variant);
 

@@ -725,58 +725,6 @@ __device__ __forceinline__ void bend_eval_grid(float4 a0, float4 a1, float4 a2, 
     c3 = make_float4(k3.x, k3.y, k3.z, 1.0f);
 }
 
-// The two halves of grid_generator (below), for kernels that run them on separate
-// threads: the stretch constraints t0..t3 of generator (X, Y) into sst (returning t3's
-// length, the bend's shared-edge length, 0 outside the cloth) and the bend of quad (X, Y)
-// into sbd.  The same operations as grid_generator, so the same bits.
-template <int kHB, int kGA, int kGB>
-__device__ __forceinline__ float grid_generator_stretch(int X, int Y, int R, const float4 (*sp)[kHB], int hx, int hy,
-                                                        float4 (*sst)[kGA][kGB], int gx, int gy, float4 rest)
-{
-    const float4 zero = make_float4(0, 0, 0, 0);
-    const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
-    const bool full = gen && X < R && Y < R;
-    const float4 pxy = sp[hx][hy];
-    vec3 cm;
-    float4 r = zero;
-    if (gen && Y < R && stretch_common(pxy, sp[hx][hy + 1], rest.x, cm))  // t0: (x,y)-(x,y+1)
-        r = make_float4(cm.x, cm.y, cm.z, 1.0f);
-    sst[0][gx][gy] = r;
-    r = zero;
-    if (gen && X < R && stretch_common(pxy, sp[hx + 1][hy], rest.y, cm))  // t1: (x,y)-(x+1,y)
-        r = make_float4(cm.x, cm.y, cm.z, 1.0f);
-    sst[1][gx][gy] = r;
-    r = zero;
-    if (full && stretch_common(pxy, sp[hx + 1][hy + 1], rest.z, cm))  // t2: (x,y)-(x+1,y+1)
-        r = make_float4(cm.x, cm.y, cm.z, 1.0f);
-    sst[2][gx][gy] = r;
-    r = zero;
-    float d3 = 0.0f;
-    if (full) {  // t3: (x,y+1)-(x+1,y); its length is the bend's shared-edge length
-        const float4 a01 = sp[hx][hy + 1], a10 = sp[hx + 1][hy];
-        const vec3 e3 = xyz(a01) - xyz(a10);
-        d3 = length_exact(e3);
-        if (stretch_common_d(e3, d3, a01.w, a10.w, rest.w, cm)) r = make_float4(cm.x, cm.y, cm.z, 1.0f);
-    }
-    sst[3][gx][gy] = r;
-    return d3;
-}
-
-template <int kHB, int kGA, int kGB>
-__device__ __forceinline__ void grid_generator_bend(int X, int Y, int R, const float4 (*sp)[kHB], int hx, int hy,
-                                                    float4 (*sbd)[kGA][kGB], int gx, int gy, float d3, float xpbd)
-{
-    const float4 zero = make_float4(0, 0, 0, 0);
-    const bool full = X >= 0 && Y >= 0 && X < R && Y < R;
-    float4 c0 = zero, c1 = zero, c2 = zero, c3 = zero;
-    if (full)
-        bend_eval_grid(sp[hx][hy], sp[hx + 1][hy + 1], sp[hx][hy + 1], sp[hx + 1][hy], d3, 0.0f, xpbd, c0, c1, c2, c3);
-    sbd[0][gx][gy] = c0;
-    sbd[1][gx][gy] = c1;
-    sbd[2][gx][gy] = c2;
-    sbd[3][gx][gy] = c3;
-}
-
 // Generator (X, Y) of a grid cloth of R x R quads: its stretch constraints t0..t3 (rests
 // rest.x .. rest.w) and the bend of quad (X, Y), from the predicted position of (X, Y) at
 // sp[hx][hy] and of (X,Y+1), (X+1,Y), (X+1,Y+1) beside it.  Each stretch result goes to
@@ -1132,15 +1080,13 @@ k_grid_substep_cluster(const GridTile* __restrict__ tiles, const int2* __restric
 // barrier (release / acquire) between iterations publishes those stores.  Global memory
 // is read once per substep (positions, rests, attachments) and written once (the last
 // iteration's finalize).  Generators and particle sums are the tile kernel's functions
-// on the same values, so the results are its bits.  640 threads: the 17 x 17 generators'
-// stretch constraints on threads 0..288 and their bends on threads 320..608 (the two
-// halves of a generator run side by side, so an iteration waits on the bend's chain
-// alone), the 16 x 16 particles on threads 0..255.
+// on the same values, so the results are its bits (the fast build included: the
+// generator is the tile kernel's grid_generator, whole, so its contracted arithmetic is
+// the same).  320 threads: 17 x 17 generators, 16 x 16 particles.
 constexpr int kResT = 16;
-constexpr int kResHalf = 320;  // the bend half of the threads starts here
-constexpr int kResThreads = 2 * kResHalf;
+constexpr int kResThreads = 320;
 constexpr int kResHalo = kResT + 2, kResGen = kResT + 1;
-static_assert(kResGen * kResGen <= kResHalf && kResT * kResT <= kResHalf, "threads cover the tile");
+static_assert(kResGen * kResGen <= kResThreads && kResT * kResT <= kResThreads, "threads cover the tile");
 static_assert(kClusterCtas == 16, "a 4 x 4 grid of tiles");
 
 struct ResidentSmem {
@@ -1191,8 +1137,7 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
     // generators (a0 - 1 + gx, b0 - 1 + gy): the 15 x 15 interior ones (no halo position
     // read) first, then the 64 on the border; warps whose generators are all interior
     // compute before waiting for the neighbours' halo stores
-    const bool bend_half = tid >= kResHalf;
-    const int g = bend_half ? tid - kResHalf : tid;
+    const int g = tid;
     constexpr int kInner = (kResGen - 2) * (kResGen - 2);
     int gx, gy;
     if (g < kInner) {
@@ -1215,7 +1160,7 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
         }
     }
     const bool has_gen = g < kResGen * kResGen;
-    const bool inner_warp = ((tid >> 5) % (kResHalf / 32)) * 32 + 31 < kInner;
+    const bool inner_warp = (tid >> 5) * 32 + 31 < kInner;
     const int ta = tid / kResT, tb = tid - ta * kResT;     // particle (a0 + ta, b0 + tb)
     const int a = a0 + ta, b = b0 + tb;
     const int i = base + a * V + b;
@@ -1235,7 +1180,7 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
             cp_async16_zfill(&S.sp[0][ha][hb], pin + (in ? base + pa * V + pb : base), in);
             S.sp[1][ha][hb] = make_float4(0, 0, 0, 0);
         }
-        if (has_gen && !bend_half) {
+        if (has_gen) {
             const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
             const bool gen = X >= 0 && Y >= 0 && X <= R && Y <= R;
             cp_async16_zfill(&S.sgr[g], grest + (gen ? base + X * V + Y : base), gen);
@@ -1261,19 +1206,9 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
         // the previous iteration's halo stores are published by the cluster barrier it
         // arrived at; interior generators read only this block's positions
         if (it > 0 && !inner_warp) cluster_wait();
-        if (active && has_gen) {
-            const int X = a0 - 1 + gx, Y = b0 - 1 + gy;
-            if (!bend_half) {
-                grid_generator_stretch<kResHalo, kResGen, kResGen>(X, Y, R, S.sp[cur], gx, gy, S.sst, gx, gy,
-                                                                   S.sgr[g]);
-            } else {
-                // t3's length with the stretch half's operations
-                const bool full = X >= 0 && Y >= 0 && X < R && Y < R;
-                const float d3 = full ? length_exact(xyz(S.sp[cur][gx][gy + 1]) - xyz(S.sp[cur][gx + 1][gy])) : 0.0f;
-                grid_generator_bend<kResHalo, kResGen, kResGen>(X, Y, R, S.sp[cur], gx, gy, S.sbd, gx, gy, d3,
-                                                                D.xpbd_bend);
-            }
-        }
+        if (active && has_gen)
+            grid_generator<kResHalo, kResGen, kResGen>(a0 - 1 + gx, b0 - 1 + gy, R, S.sp[cur], gx, gy, S.sst,
+                                                       S.sbd, gx, gy, S.sgr[g], D.xpbd_bend);
         if (it > 0 && inner_warp) cluster_wait();
         __syncthreads();
         if (owns) {

@@ -309,7 +309,9 @@ vt_status upload_tables(vt_server* s, cudaStream_t st)
 {
     std::vector<vt::Tile> pt, gpt;
     std::vector<vt::GridTile> gt;
-    s->grid_variant = vt::last_tuned_variant();
+    // the tile shape the batched mix tunes to (15x15, four blocks per SM), or the one
+    // vt_tuning_set_grid_tile forces: never the last shape some other solver tuned to
+    s->grid_variant = vt::grid_variant_for(vt::kGridDefaultVariant);
     for (int32_t sid = 0; sid < (int32_t)s->slot.size(); ++sid) {
         const Request* r = s->slot[sid];
         if (!r) continue;

@@ -175,7 +175,6 @@ vt_status profiler_read(vt_stage_time* out, uint32_t cap, uint32_t* count)
 namespace {
 std::mutex g_tune_mu;
 int g_forced_variant = -1;
-int g_last_tuned = kGridDefaultVariant;
 std::vector<std::pair<std::vector<int64_t>, int>> g_tune_cache;  // signature -> variant
 }  // namespace
 
@@ -183,12 +182,6 @@ int grid_variant_for(int tuned)
 {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     return g_forced_variant >= 0 ? g_forced_variant : tuned;
-}
-
-int last_tuned_variant()
-{
-    std::lock_guard<std::mutex> lock(g_tune_mu);
-    return g_forced_variant >= 0 ? g_forced_variant : g_last_tuned;
 }
 
 // ------------------------------------------------------------------ tensor maps
@@ -474,7 +467,6 @@ vt_status World::autotune(cudaStream_t st, bool may_time)
         cudaEventDestroy(e1);
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune_cache.push_back({sig, best});
-        g_last_tuned = best;
     }
     return best == grid_variant ? VT_OK : set_grid_variant(best);
 }
