@@ -286,21 +286,13 @@ k_rs_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin
     }
 }
 
-// All passes of a sort that fits one tile (n <= 4096) in one block: the pairs stay in
-// shared memory between passes, and each pass's digit offsets are the tile's own prefix
-// sums, so no count kernel, look-back or scratch is needed.  Same ranking as
-// k_rs_onesweep, so the same stable order.
-__global__ void __launch_bounds__(kBlock)
-k_rs_single_tile(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
-                 uint32_t* __restrict__ vout, int32_t n, int passes, int per, int bits, int32_t* __restrict__ status)
+// All passes of a sort that fits one tile (n <= 4096) on one block, the pairs in shared
+// memory (sk, sv) from before the call to after it: each pass's digit offsets are the
+// tile's own prefix sums, so no count kernel, look-back or scratch is needed.  Same
+// ranking as k_rs_onesweep, so the same stable order.  Ends with a block barrier.
+__device__ __forceinline__ void tile_sort_smem(uint32_t* sk, uint32_t* sv, int32_t n, int passes, int per, int bits,
+                                               uint32_t (*wcnt)[256], uint32_t* lofs, int32_t* status)
 {
-    __shared__ uint32_t lofs[256];
-    __shared__ uint32_t wcnt[kRsWarps][256];
-    __shared__ uint32_t sk[kRsTile], sv[kRsTile];
-    for (int k = threadIdx.x; k < n; k += kBlock) {
-        sk[k] = kin[k];
-        sv[k] = vin[k];
-    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1u;
     const int wbase = warp * (32 * kRsItems);
@@ -357,6 +349,22 @@ k_rs_single_tile(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ 
         shift += nb;
         __syncthreads();  // the pass's pairs are placed and its counters read
     }
+    __syncthreads();  // the sorted pairs are in place (also when there is no pass)
+}
+
+// The one-tile sort as a kernel (radix_sort_pairs for n <= 4096).
+__global__ void __launch_bounds__(kBlock)
+k_rs_single_tile(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+                 uint32_t* __restrict__ vout, int32_t n, int passes, int per, int bits, int32_t* __restrict__ status)
+{
+    __shared__ uint32_t lofs[256];
+    __shared__ uint32_t wcnt[kRsWarps][256];
+    __shared__ uint32_t sk[kRsTile], sv[kRsTile];
+    for (int k = threadIdx.x; k < n; k += kBlock) {
+        sk[k] = kin[k];
+        sv[k] = vin[k];
+    }
+    tile_sort_smem(sk, sv, n, passes, per, bits, wcnt, lofs, status);
     for (int k = threadIdx.x; k < n; k += kBlock) {
         kout[k] = sk[k];
         vout[k] = sv[k];
@@ -449,6 +457,71 @@ cudaError_t launch_cell_ranges_gather(const DeviceArrays& d, int pin, int32_t n,
     if (n <= 0) return cudaSuccess;
     k_cell_ranges_gather<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(d.keys, d.vals, d.p[pin], d.x0, n,
                                                                       d.cells, d.ps, d.x0s, d.status);
+    return cudaGetLastError();
+}
+
+// The whole hash of a small world (kHashOneTileMaxParticles, within one sort tile), up
+// to the neighbour walk, on one block: the cell table cleared, every particle's key, the sort in
+// shared memory, the cell ranges and the sorted copies — what the table clear,
+// k_hash_keys, the sort and k_cell_ranges_gather do in four launches, with the same
+// results.  The sort's pass count is the one radix_sort_pairs takes.
+__global__ void __launch_bounds__(kBlock)
+k_hash_one_tile(const Tile* __restrict__ tiles, int32_t n_ptiles, const DomainParams* __restrict__ doms,
+                const float4* __restrict__ p, const float4* __restrict__ x0, int32_t n, int passes, int per,
+                int bits, int32_t total_keys, uint2* __restrict__ cells, uint32_t* __restrict__ keys,
+                uint32_t* __restrict__ vals, float4* __restrict__ ps, float4* __restrict__ x0s,
+                int32_t* __restrict__ status)
+{
+    __shared__ uint32_t lofs[256];
+    __shared__ uint32_t wcnt[kRsWarps][256];
+    __shared__ uint32_t sk[kRsTile], sv[kRsTile];
+    const int tid = (int)threadIdx.x;
+    for (int k = tid; k < total_keys; k += kBlock) cells[k] = make_uint2(0xffffffffu, 0xffffffffu);
+    for (int t = 0; t < n_ptiles; ++t) {
+        const Tile tl = tiles[t];
+        const int i = tl.begin + tid;
+        if (i < tl.end && VT_IN_RANGE(i, 0, n, status)) {
+            const DomainParams& D = doms[tl.dom];
+            const float4 q = p[i];
+            const float sp = D.cell_spacing;
+            sk[i] = (uint32_t)D.table_base +
+                    hash_coords(int_coord(q.x, sp), int_coord(q.y, sp), int_coord(q.z, sp), D.table_size);
+            sv[i] = (uint32_t)i;
+        }
+    }
+    // sorts, and orders the clear above before the range stores below
+    tile_sort_smem(sk, sv, n, passes, per, bits, wcnt, lofs, status);
+    for (int t = tid; t < n; t += kBlock) {
+        const uint32_t h = sk[t];
+        if (t == 0 || sk[t - 1] != h) {
+            cells[h].x = (uint32_t)t;
+            if (t > 0) cells[sk[t - 1]].y = (uint32_t)t;
+        }
+        if (t == n - 1) cells[h].y = (uint32_t)n;
+        const uint32_t id = sv[t];
+        keys[t] = h;
+        vals[t] = id;
+        if (!VT_IN_RANGE(id, 0, n, status)) continue;
+        const float4 q = p[id];
+        ps[t] = make_float4(q.x, q.y, q.z, __uint_as_float(id));
+        x0s[t] = x0[id];
+    }
+}
+
+static_assert(kHashOneTileMaxParticles <= kRsTile, "the one-block hash sorts one tile");
+
+bool hash_one_tile(int32_t n, int32_t total_keys)
+{
+    return n >= 1 && n <= kHashOneTileMaxParticles && total_keys <= kHashOneTileMaxKeys;
+}
+
+cudaError_t launch_hash_one_tile(const Launch& L, int pin, int32_t bits, int32_t total_keys)
+{
+    const DeviceArrays& d = *L.d;
+    const int passes = radix_passes(L.n_particles, bits);
+    const int per = passes ? (bits + passes - 1) / passes : 0;
+    k_hash_one_tile<<<1, kBlock, 0, L.st>>>(d.ptiles, L.n_ptiles, d.dom, d.p[pin], d.x0, L.n_particles, passes, per,
+                                            bits, total_keys, d.cells, d.keys, d.vals, d.ps, d.x0s, d.status);
     return cudaGetLastError();
 }
 

@@ -125,11 +125,6 @@ public:
     vt_status read_status(std::vector<int32_t>& flags, cudaStream_t st);
     vt_status clear_status(cudaStream_t st);
 
-    // Launch count of one frame with these arguments (for the bench's gpu_launches).
-    static int64_t launches_per_frame(int32_t substeps, int32_t iterations, int32_t ih,
-                                      bool self, bool bends, int32_t n_particles,
-                                      int32_t total_keys);
-
     DeviceArrays d;
     std::vector<DomainParams> hdom;
     std::vector<ColliderDev> hcol;

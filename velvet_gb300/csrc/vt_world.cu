@@ -882,22 +882,6 @@ vt_status World::set_slot(int k, int32_t slot, const float xyz[3])
     return VT_OK;
 }
 
-int64_t World::launches_per_frame(int32_t S, int32_t It, int32_t ih, bool self, bool bends,
-                                  int32_t n, int32_t tk)
-{
-    int64_t L = 1 + 1;  // presdf_predict + normals
-    int bits = 0;
-    while ((1ll << bits) < (int64_t)tk) ++bits;
-    const int sort = radix_launches(n, bits);
-    for (int s = 0; s < S; ++s) {
-        if (self && s % ih == 0) L += 3 + sort;  // keys, ranges, cache + sort
-        L += 1;                                         // collide
-        L += (int64_t)It * (bends ? 2 : 1);
-        if (It == 0) L += 1;
-    }
-    return L;
-}
-
 vt_status World::simulate(const FrameArgs& a, int32_t ih, bool any_self, cudaStream_t st,
                           bool use_graph)
 {
@@ -988,13 +972,17 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
     VT_STAGE(ST_PRESDF_PREDICT, launch_presdf_predict(L, pc), "presdf_predict", pk);
     for (int sub = 0; sub < a.substeps; ++sub) {
         if (any_self && sub % ih == 0) {
-            VT_CUDA(cudaMemsetAsync(d.cells, 0xff, (size_t)total_keys * sizeof(uint2), st), "memset cells");
-            VT_STAGE(ST_HASH_KEYS, launch_hash_keys(L, pc, sort_odd), "hash_keys", pk);
-            VT_STAGE(ST_RADIX_SORT,
-                     radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, n_particles,
-                                      bits, st, d.status),
-                     "radix_sort", (uint64_t)radix_launches(n_particles, bits));
-            VT_STAGE(ST_CELL_RANGES, launch_cell_ranges_gather(d, pc, n_particles, st), "cell_ranges", 1);
+            if (hash_one_tile(n_particles, total_keys)) {
+                VT_STAGE(ST_HASH_KEYS, launch_hash_one_tile(L, pc, bits, total_keys), "hash_one_tile", 1);
+            } else {
+                VT_CUDA(cudaMemsetAsync(d.cells, 0xff, (size_t)total_keys * sizeof(uint2), st), "memset cells");
+                VT_STAGE(ST_HASH_KEYS, launch_hash_keys(L, pc, sort_odd), "hash_keys", pk);
+                VT_STAGE(ST_RADIX_SORT,
+                         radix_sort_pairs(d.keys, d.vals, d.keys_tmp, d.vals_tmp, d.hist, n_particles,
+                                          bits, st, d.status),
+                         "radix_sort", (uint64_t)radix_launches(n_particles, bits));
+                VT_STAGE(ST_CELL_RANGES, launch_cell_ranges_gather(d, pc, n_particles, st), "cell_ranges", 1);
+            }
             VT_STAGE(ST_CACHE_NEIGHBORS, launch_cache_neighbors(L, pc), "cache_neighbors", pk);
         }
         VT_STAGE(ST_COLLIDE, launch_collide(L, pc, 1 - pc), "collide", pk);

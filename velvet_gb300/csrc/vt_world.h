@@ -252,6 +252,15 @@ cudaError_t launch_render(const float4* x, int64_t n, const vt_render_params& rp
 // contiguous copy instead of a copy of 12-byte rows out of 16-byte ones.
 // Cell start/end of the sorted keys plus ps / x0s (positions in sorted-slot order).
 cudaError_t launch_cell_ranges_gather(const DeviceArrays& d, int pin, int32_t n, cudaStream_t st);
+// A world of at most kHashOneTileMaxParticles particles hashes in one launch
+// (k_hash_one_tile: table clear, keys, sort, cell ranges, sorted copies on one block) when
+// its cell table has at most kHashOneTileMaxKeys buckets.  One block does the work of the
+// four launches' many: a 32x32 cloth's frame 0.231 -> 0.220 ms, a 64x64 one's 0.243 ->
+// 0.264 ms, so larger worlds keep the four launches.
+constexpr int32_t kHashOneTileMaxParticles = 2048;
+constexpr int32_t kHashOneTileMaxKeys = 1 << 16;
+bool hash_one_tile(int32_t n, int32_t total_keys);
+cudaError_t launch_hash_one_tile(const Launch& L, int pin, int32_t bits, int32_t total_keys);
 cudaError_t launch_pack_xyz(const float4* src, float* dst, int64_t n, cudaStream_t st);
 
 // One Jacobi iteration of the grid domains (stretch + attach + bending + ApplyDeltas,
