@@ -784,6 +784,7 @@ vt_status vt_solver_debug_get(vt_solver* s, int32_t what, void* dst, uint64_t by
     case VT_DEBUG_PARTICLE_INDEX: src = d.vals; need = 4 * n; break;
     case VT_DEBUG_CELL_START: need = 4 * (T + 1); break;
     case VT_DEBUG_CELL_END: need = 4 * T; break;
+    // the lists are kept in the reference's layout (particle id's list in column id)
     case VT_DEBUG_NEIGHBORS: src = d.nbr; need = 4 * n * (uint64_t)s->h.P.max_num_neighbors; break;
     case VT_DEBUG_PREDICTED: need = 12 * n; break;
     default: vt::set_error("unknown debug view"); return VT_ERR_INVALID_ARGUMENT;
@@ -800,24 +801,6 @@ vt_status vt_solver_debug_get(vt_solver* s, int32_t what, void* dst, uint64_t by
         const uint64_t rows = what == VT_DEBUG_CELL_END ? T : T + 1;
         if (rows) VT_TRY_CUDA(cudaMemcpy2D(dst, 4, col, 8, 4, rows, cudaMemcpyDeviceToHost), "copy");
         return VT_OK;
-    }
-    if (what == VT_DEBUG_NEIGHBORS && n) {
-        // the device keeps the lists in sorted-slot order (column t = the particle in
-        // sorted slot t); the reference's layout puts particle id's list in column id
-        VT_GUARD_BEGIN
-        const uint64_t mn = (uint64_t)s->h.P.max_num_neighbors;
-        std::vector<uint32_t> lists(n * mn), order(n);
-        VT_TRY_CUDA(cudaMemcpy(lists.data(), d.nbr, 4 * n * mn, cudaMemcpyDeviceToHost), "copy");
-        VT_TRY_CUDA(cudaMemcpy(order.data(), d.vals, 4 * n, cudaMemcpyDeviceToHost), "copy");
-        uint32_t* out = static_cast<uint32_t*>(dst);
-        std::memset(out, 0xff, 4 * n * mn);
-        for (uint64_t t = 0; t < n; ++t) {
-            const uint64_t id = order[t];
-            if (id >= n) continue;
-            for (uint64_t k = 0; k < mn; ++k) out[id + k * n] = lists[t + k * n];
-        }
-        return VT_OK;
-        VT_GUARD_END
     }
     if (need) VT_TRY_CUDA(cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost), "copy");
     return VT_OK;

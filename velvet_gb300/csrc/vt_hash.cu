@@ -584,14 +584,17 @@ __device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* 
 // The same walk over sorted-slot copies of the positions: candidate k is ps[k] (its
 // position, its index in w) and x0s[k], one 16-byte load each, contiguous within a
 // bucket; the thread's own object is slot t, so the threads of a warp share buckets.
-// Same arithmetic, order and caps.  The list is written in sorted-slot order (column
-// t - slot_base of the domain's block), so a warp's stores of entry k are consecutive
-// words; the collision pass reads the lists in the same order.  (Measured alternatives:
+// Same arithmetic, order and caps.  The list goes to column id - id_base of the domain's
+// block (the reference's neighbors[id + k N]), so the collision pass, one thread per
+// particle, reads entry k of consecutive particles' lists as consecutive words.  (Lists
+// in sorted-slot order, the walk's own thread order, made these stores consecutive but
+// cost the collision pass a gather of each particle's own state: 1.36 -> 1.66 ms per
+// frame of the mix against no gain in the walk.)  Measured forms of the walk itself:
 // threads in object order, a warp per object, a warp per cell group, (start, end) pairs
 // loaded three buckets at a time, and the next bucket's range loaded ahead with
 // candidates loaded two or four at a time all ran slower — the walk is bound by load
 // latency, and this form's 32 registers give the highest occupancy and the most shared
-// bucket reads.)
+// bucket reads.
 __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint2* __restrict__ cells,
                                                        const float4* __restrict__ ps,
                                                        const float4* __restrict__ x0s,
@@ -607,7 +610,7 @@ __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint2* 
     const int32_t ix = int_coord(position.x, sp), iy = int_coord(position.y, sp),
                   iz = int_coord(position.z, sp);
     if (!VT_IN_RANGE(t, slot_base, (long long)slot_base + n, status)) return;
-    uint32_t* out = out_base + (t - slot_base);
+    uint32_t* out = out_base + (id - id_base);
     // the 27 keys are XORs of per-axis products: (x+dx)*A etc. wrap like x*A
     uint32_t hx[3], hy[3], hz[3];
 #pragma unroll
@@ -752,7 +755,7 @@ k_cache_neighbors_warp(const Tile* __restrict__ tiles, const DomainParams* __res
         if (lane >= o) incl += u;
     }
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    uint32_t* out = nbr + nbr_offset(D) + (slot - sbase);
+    uint32_t* out = nbr + nbr_offset(D) + (id - id_base);
     uint32_t pos = incl - cnt;
     if (cnt && pos < (uint32_t)max_nbr) {
         for (uint32_t k = start; k < end && pos < (uint32_t)max_nbr; ++k) {

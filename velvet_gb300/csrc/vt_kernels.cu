@@ -229,30 +229,23 @@ k_presdf_predict(const Tile* __restrict__ tiles, const DomainParams* __restrict_
 
 // ------------------------------------------------------------------ collide particles + SDF
 // CollideParticles_Kernel (VtClothSolverGPU.cu:329-373) + ApplyDeltas (:253-264) +
-// CollideSDF (:289-314) for one substep.  With self-collision the threads take the
-// domain's particles in sorted-slot order (thread r of the domain: the particle in its
-// r-th sorted slot), so each thread's neighbour list is column r and a warp reads entry
-// k of 32 lists as consecutive words; a particle's result does not depend on which
-// thread computes it.
+// CollideSDF (:289-314) for one substep.  Thread r of a domain takes the domain's r-th
+// particle, whose neighbour list is column r, so a warp reads entry k of 32 lists and
+// its own particles' positions as consecutive words.
 constexpr int kCollideBatch = 4;  // list entries gathered together (2 / 8 / 16: 1.67 / 1.91 / 2.67 vs 1.66 ms per mix frame)
 
 __global__ void __launch_bounds__(kBlock)
 k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
           const ColliderDev* __restrict__ cols, const float4* __restrict__ x,
           const float4* __restrict__ pin, float4* __restrict__ pout,
-          const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ vals,
-          const int32_t* __restrict__ dslot, int32_t* __restrict__ status)
+          const uint32_t* __restrict__ nbr, int32_t* __restrict__ status)
 {
     const Tile tl = tiles[blockIdx.x];
     const int t = tl.begin + (int)threadIdx.x;
     if (t >= tl.end) return;
     const DomainParams& D = doms[tl.dom];
-    const int r = t - D.p_begin;  // rank within the domain
-    int i = t;
-    if (D.self_collision) {
-        i = (int)vals[(dslot ? dslot[tl.dom] : D.p_begin) + r];
-        if (!VT_IN_RANGE(i, D.p_begin, D.p_begin + D.p_count, status)) return;
-    }
+    const int r = t - D.p_begin;  // rank within the domain: the list's column
+    const int i = t;
     const float4 pi4 = pin[i];
     vec3 pi = xyz(pi4);
     const float wi = pi4.w;
@@ -1378,8 +1371,7 @@ cudaError_t launch_collide(const Launch& L, int pin, int pout)
 {
     if (!L.n_ptiles) return cudaSuccess;
     const DeviceArrays& d = *L.d;
-    k_collide<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.col, d.x, d.p[pin], d.p[pout], d.nbr, d.vals,
-                                               d.dslot, d.status);
+    k_collide<<<L.n_ptiles, kBlock, 0, L.st>>>(d.ptiles, d.dom, d.col, d.x, d.p[pin], d.p[pout], d.nbr, d.status);
     return cudaGetLastError();
 }
 

@@ -21,10 +21,9 @@
 //               corner slots per particle in constraint order
 //   normals     tn_off/tn_ent CSR of triangles per vertex; tri uint4 per triangle
 //   hash        keys/vals (sorted pairs), cells (start, end) per bucket (sum of (T_d + 1)),
-//               neighbours (max_nbr * n_d per domain, column-major inside a domain, in
-//               sorted-slot order: the list of the particle in the domain's r-th sorted
-//               slot is column r, so the walk that writes the lists and the collision
-//               pass that reads them both run in sorted order and access whole rows)
+//               neighbours (max_nbr * n_d per domain, column-major inside a domain: the
+//               list of the domain's r-th particle is column r, the reference's
+//               neighbors[id + k N], read by the collision pass in particle order)
 #pragma once
 
 #include <cstdint>
