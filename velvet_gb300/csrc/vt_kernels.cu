@@ -234,18 +234,14 @@ k_presdf_predict(const Tile* __restrict__ tiles, const DomainParams* __restrict_
 // its own particles' positions as consecutive words.
 constexpr int kCollideBatch = 4;  // list entries gathered together (2 / 8 / 16: 1.67 / 1.91 / 2.67 vs 1.66 ms per mix frame)
 
-__global__ void __launch_bounds__(kBlock)
-k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
-          const ColliderDev* __restrict__ cols, const float4* __restrict__ x,
-          const float4* __restrict__ pin, float4* __restrict__ pout,
-          const uint32_t* __restrict__ nbr, int32_t* __restrict__ status)
+// Particle i (the domain's r-th) after its collisions, ApplyDeltas and the SDF: its
+// predicted position from pin, the other particles' from pin too (every particle reads the
+// positions from before the pass), velocities against x.  Returns (position, inverse mass).
+__device__ __forceinline__ float4 collide_particle(const DomainParams& D, const ColliderDev* __restrict__ cols,
+                                                   int i, int r, const float4* __restrict__ x,
+                                                   const float4* __restrict__ pin, const uint32_t* __restrict__ nbr,
+                                                   int32_t* __restrict__ status)
 {
-    const Tile tl = tiles[blockIdx.x];
-    const int t = tl.begin + (int)threadIdx.x;
-    if (t >= tl.end) return;
-    const DomainParams& D = doms[tl.dom];
-    const int r = t - D.p_begin;  // rank within the domain: the list's column
-    const int i = t;
     const float4 pi4 = pin[i];
     vec3 pi = xyz(pi4);
     const float wi = pi4.w;
@@ -304,7 +300,20 @@ k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
         }
     }
     pi = collide_sdf(D, cols, pi, xi, D.dt_sub);
-    pout[i] = make_float4(pi.x, pi.y, pi.z, wi);
+    return make_float4(pi.x, pi.y, pi.z, wi);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
+          const ColliderDev* __restrict__ cols, const float4* __restrict__ x,
+          const float4* __restrict__ pin, float4* __restrict__ pout,
+          const uint32_t* __restrict__ nbr, int32_t* __restrict__ status)
+{
+    const Tile tl = tiles[blockIdx.x];
+    const int t = tl.begin + (int)threadIdx.x;
+    if (t >= tl.end) return;
+    const DomainParams& D = doms[tl.dom];
+    pout[t] = collide_particle(D, cols, t, t - D.p_begin, x, pin, nbr, status);
 }
 
 // ------------------------------------------------------------------ constraint math
@@ -1111,8 +1120,9 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
                         float4* __restrict__ p0, float4* __restrict__ p1, float4* __restrict__ x,
                         float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ grest,
                         const float4* __restrict__ glra, const float4* __restrict__ slots,
-                        const float4* __restrict__ slots0, int32_t* __restrict__ status, int pin0,
-                        int iterations, int last_substep)
+                        const float4* __restrict__ slots0, const ColliderDev* __restrict__ cols,
+                        const uint32_t* __restrict__ nbr, int32_t* __restrict__ status, int pin0,
+                        int iterations, int last_substep, int with_collide)
 {
     extern __shared__ __align__(128) unsigned char res_smem[];
     ResidentSmem& S = *reinterpret_cast<ResidentSmem*>(res_smem);
@@ -1166,12 +1176,14 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
     const bool stage_lra = ns >= 1 && ns <= kGridLraCached;
 
     // stage the tile and halo (zero outside the cloth; the next buffer's halo starts at
-    // zero and stays so outside the cloth), the rests, the attachments and x
+    // zero and stays so outside the cloth), the rests, the attachments and x.  With the
+    // collision pass folded in, the first buffer starts at zero too and takes the
+    // collision results below.
     if (active) {
         for (int k = tid; k < kResHalo * kResHalo; k += kResThreads) {
             const int ha = k / kResHalo, hb = k - ha * kResHalo;
             const int pa = a0 - 1 + ha, pb = b0 - 1 + hb;
-            const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V;
+            const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V && !with_collide;
             cp_async16_zfill(&S.sp[0][ha][hb], pin + (in ? base + pa * V + pb : base), in);
             S.sp[1][ha][hb] = make_float4(0, 0, 0, 0);
         }
@@ -1192,10 +1204,33 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
         ngroups = (ns + gsize - 1) / gsize;
         lra_group_boxes(S.sgl, S.ssup, slots + s0, slots0 + s0, ns, gsize, ngroups, tid);
     }
-    // every block's next buffer is cleared before any neighbour stores into it
+    // every block's buffers are cleared before any neighbour stores into them
     cluster_barrier();
 
-    int pc = pin0;
+    // the substep's collision pass (k_collide's work for this tile: every particle reads
+    // the positions from before the pass, in global memory), its results into the first
+    // buffer and the neighbours' halos
+    if (with_collide) {
+        if (owns) {
+            const float4 q = collide_particle(D, cols, i, i - D.p_begin, x, pin, nbr, status);
+            const int hx = ta + 1, hy = tb + 1;
+            S.sp[0][hx][hy] = q;
+            const bool up = ta == 0 && rt > 0, down = ta == kResT - 1 && rt < 3;
+            const bool left = tb == 0 && rc > 0, right = tb == kResT - 1 && rc < 3;
+            if (up) st_cluster_f4(&S.sp[0][kResT + 1][hy], (uint32_t)(rank - 4), q);
+            if (down) st_cluster_f4(&S.sp[0][0][hy], (uint32_t)(rank + 4), q);
+            if (left) st_cluster_f4(&S.sp[0][hx][kResT + 1], (uint32_t)(rank - 1), q);
+            if (right) st_cluster_f4(&S.sp[0][hx][0], (uint32_t)(rank + 1), q);
+            if (up && left) st_cluster_f4(&S.sp[0][kResT + 1][kResT + 1], (uint32_t)(rank - 5), q);
+            if (up && right) st_cluster_f4(&S.sp[0][kResT + 1][0], (uint32_t)(rank - 3), q);
+            if (down && left) st_cluster_f4(&S.sp[0][0][kResT + 1], (uint32_t)(rank + 3), q);
+            if (down && right) st_cluster_f4(&S.sp[0][0][0], (uint32_t)(rank + 5), q);
+        }
+        cluster_barrier();  // publishes the halo stores
+    }
+
+    // the iterations' first input is the collision pass's output buffer
+    int pc = with_collide ? pin0 ^ 1 : pin0;
     for (int it = 0; it < iterations; ++it) {
         const int cur = it & 1;
         // the previous iteration's halo stores are published by the cluster barrier it
@@ -1555,7 +1590,7 @@ static cudaLaunchConfig_t resident_config(const Launch& L, int n_cloths, cudaLau
 }
 
 cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom, int n_cloths, int pin,
-                                         int iterations, int last_sub)
+                                         int iterations, int last_sub, int with_collide)
 {
     if (n_cloths <= 0 || iterations <= 0) return cudaSuccess;
     const DeviceArrays& d = *L.d;
@@ -1563,7 +1598,8 @@ cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom,
     const cudaLaunchConfig_t cfg = resident_config(L, n_cloths, at);
     return cudaLaunchKernelEx(&cfg, k_grid_substep_resident, cloth_dom, (const DomainParams*)d.dom, d.p[0], d.p[1],
                               d.x, d.v, (const float4*)d.x0, (const float4*)d.grest, (const float4*)d.glra,
-                              (const float4*)d.slots, (const float4*)d.slots0, d.status, pin, iterations, last_sub);
+                              (const float4*)d.slots, (const float4*)d.slots0, (const ColliderDev*)d.col,
+                              (const uint32_t*)d.nbr, d.status, pin, iterations, last_sub, with_collide);
 }
 
 bool substep_resident_supported()
