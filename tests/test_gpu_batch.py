@@ -47,6 +47,37 @@ def test_batch_equals_each_cloth_alone(graphs):
         assert np.array_equal(bits(batch.normals(k)), bits(o.normals())), f"cloth {k} normals"
 
 
+@pytest.mark.skipif(_abi.VARIANT == "fast", reason="bits of the oracle / host arithmetic: exact build only")
+def test_batch_of_tiny_cloths_matches_the_oracle():
+    """Five cloths of 8-16 particles a side, 2,048 particles at most in all: the whole
+    hash on one block (several domains' keys, one sort, their cell ranges), the
+    warp-per-particle neighbour walk and the cluster-resident substeps with the collision
+    pass folded in, one cluster per cloth — each cloth the oracle's bits."""
+    wl = W.batched(5, frames=6, seed=21, lo=8, hi=16)
+    assert sum(c.num_particles for c in wl.cloths) <= 2048
+    batch = vg.BatchSolver()
+    ors = []
+    for spec in wl.cloths:
+        s = vg.ClothSolver()
+        W.build_plain(spec, s)
+        batch.add(s)
+        s.close()
+        o = Oracle()
+        W.build_plain(spec, o)
+        ors.append((o, spec))
+    for f in range(wl.frames):
+        batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin)
+        for o, spec in ors:
+            o.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin, spec.particle_diameter())
+    batch.sync()
+    for k, (o, spec) in enumerate(ors):
+        assert np.array_equal(bits(batch.positions(k)), bits(o.positions())), f"cloth {k} positions"
+        assert np.array_equal(bits(batch.velocities(k)), bits(o.velocities())), f"cloth {k} velocities"
+        o.close()
+
+
 def test_batch_mixing_kernel_kinds_equals_each_cloth_alone():
     """One batch holding grid cloths on the tile kernel, grid cloths on the CSR kernels
     (vt_solver_use_grid_kernel off) and a cloth whose 24 LRA slots take the slot-group
