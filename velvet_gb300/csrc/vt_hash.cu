@@ -596,7 +596,13 @@ __device__ __forceinline__ void cache_neighbors_one(uint32_t t, const uint32_t* 
 // loaded three buckets at a time, and the next bucket's range loaded ahead with
 // candidates loaded two or four at a time all ran slower — the walk is bound by load
 // latency, and this form's 32 registers give the highest occupancy and the most shared
-// bucket reads.
+// bucket reads; candidates loaded two at a time at eight blocks per SM (32 registers, a
+// few bytes spilled) took the mix's walk from 4.18 to 3.88 ms per frame, the same at 33
+// registers and six blocks to 4.58, four at a time spills 112 bytes.  The probes are
+// ~4% of the walk (0.15 ms per frame with the candidate loop removed); a flattened loop
+// over each thread's candidates of all buckets (the nonempty ranges compacted in shared
+// memory first, so a warp's lanes are not held at every bucket by the longest one) ran
+// at 4.61 ms.
 __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint2* __restrict__ cells,
                                                        const float4* __restrict__ ps,
                                                        const float4* __restrict__ x0s,
@@ -635,22 +641,31 @@ __device__ __forceinline__ void cache_neighbors_sorted(uint32_t t, const uint2* 
                 const uint32_t lim = start + (uint32_t)max_nbr;
                 if (lim < end) end = lim;
                 if (!VT_IN_RANGE(end, start, (long long)slot_end + 1, status)) continue;
-                for (uint32_t k = start; k < end; ++k) {
-                    const float4 qk = ps[k];
-                    const uint32_t nb = __float_as_uint(qk.w);
-                    if (!VT_IN_RANGE(nb, id_base, id_base + (uint32_t)n, status)) continue;
-                    const vec3 d1 = position - xyz(qk);
-                    if (nb == id) continue;
-                    if (!(dot(d1, d1) < sp2)) continue;
-                    if (!have_orig) {
-                        originalp = xyz(x0s[t]);
-                        have_orig = true;
-                    }
-                    const vec3 d2 = originalp - xyz(x0s[k]);
-                    if (dot(d2, d2) > diam2) {
-                        out[(size_t)cnt * n] = nb;
-                        ++cnt;
-                        if (cnt >= max_nbr) return;
+                // two candidates' loads in flight, then taken in order
+                for (uint32_t k = start; k < end; k += 2) {
+                    const float4 qa = ps[k];
+                    const bool two = k + 1 < end;
+                    const float4 qb = two ? ps[k + 1] : qa;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        if (u == 1 && !two) break;
+                        const float4 qk = u ? qb : qa;
+                        const uint32_t kk = k + (uint32_t)u;
+                        const uint32_t nb = __float_as_uint(qk.w);
+                        if (!VT_IN_RANGE(nb, id_base, id_base + (uint32_t)n, status)) continue;
+                        const vec3 d1 = position - xyz(qk);
+                        if (nb == id) continue;
+                        if (!(dot(d1, d1) < sp2)) continue;
+                        if (!have_orig) {
+                            originalp = xyz(x0s[t]);
+                            have_orig = true;
+                        }
+                        const vec3 d2 = originalp - xyz(x0s[kk]);
+                        if (dot(d2, d2) > diam2) {
+                            out[(size_t)cnt * n] = nb;
+                            ++cnt;
+                            if (cnt >= max_nbr) return;
+                        }
                     }
                 }
             }
@@ -671,7 +686,7 @@ struct PosF3 {
 
 // One block per particle tile (one domain).  The domain's sorted slots start at its first
 // particle's index in the world form and at dslot[domain] in the served form's arena.
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 8)
 k_cache_neighbors(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
                   const uint2* __restrict__ cells, const float4* __restrict__ ps, const float4* __restrict__ x0s,
                   uint32_t* __restrict__ nbr, const int32_t* __restrict__ dslot, int32_t* __restrict__ status)
