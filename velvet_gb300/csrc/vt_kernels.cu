@@ -233,6 +233,8 @@ k_presdf_predict(const Tile* __restrict__ tiles, const DomainParams* __restrict_
 // particle, whose neighbour list is column r, so a warp reads entry k of 32 lists and
 // its own particles' positions as consecutive words.
 constexpr int kCollideBatch = 4;  // list entries gathered together (2 / 8 / 16: 1.67 / 1.91 / 2.67 vs 1.66 ms per mix frame)
+// at six blocks per SM (40 registers, a few bytes spilled): 1.35 -> 1.06 ms per mix frame
+// against four blocks at 64 registers (five blocks: 1.14; six with two entries: 1.22)
 
 // Particle i (the domain's r-th) after its collisions, ApplyDeltas and the SDF: its
 // predicted position from pin, the other particles' from pin too (every particle reads the
@@ -303,7 +305,7 @@ __device__ __forceinline__ float4 collide_particle(const DomainParams& D, const 
     return make_float4(pi.x, pi.y, pi.z, wi);
 }
 
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 6)
 k_collide(const Tile* __restrict__ tiles, const DomainParams* __restrict__ doms,
           const ColliderDev* __restrict__ cols, const float4* __restrict__ x,
           const float4* __restrict__ pin, float4* __restrict__ pout,
