@@ -181,7 +181,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 
 // One pass: rank a tile's pairs by digit (stable), find each digit's output start from
 // the global digit counts and the look-back over earlier tiles, and scatter.
-__global__ void __launch_bounds__(kBlock)
+// (four blocks per SM: 64 registers instead of 80, 0.396 -> 0.385 ms of sorting per mix frame)
+__global__ void __launch_bounds__(kBlock, 4)
 k_rs_onesweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int32_t n, int pass, int shift,
               int nbits, uint32_t* __restrict__ hist, int32_t ntiles, int32_t* __restrict__ status)
