@@ -212,7 +212,7 @@ def test_substep_cluster_mode_out_of_range_is_refused():
 
 def test_substeps_in_clusters_cut_the_launches_of_a_small_cloth():
     """With clusters, a 32x32 cloth's frame launches one grid kernel per substep instead of
-    one per iteration; the resident form also folds in the substep's collision pass."""
+    one per iteration."""
     import ctypes as C
 
     counts = {}
@@ -231,10 +231,8 @@ def test_substeps_in_clusters_cut_the_launches_of_a_small_cloth():
             counts[clusters] = n1.value - n0.value
         finally:
             vg.lib().vt_tuning_set_substep_clusters(1)
-    # per substep: the re-staging cluster form launches the collision pass and one kernel
-    # for the ten iterations, the resident form one kernel for both
-    assert counts[0] - counts[2] == 5 * (10 - 1), counts
-    assert counts[2] - counts[1] == 5, counts
+    assert counts[0] - counts[1] == 5 * (10 - 1), counts
+    assert counts[2] == counts[1], counts
 
 
 @pytest.mark.parametrize("variant", [-1, 1, 5])

@@ -1123,9 +1123,8 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
                         float4* __restrict__ p0, float4* __restrict__ p1, float4* __restrict__ x,
                         float4* __restrict__ v, const float4* __restrict__ x0, const float4* __restrict__ grest,
                         const float4* __restrict__ glra, const float4* __restrict__ slots,
-                        const float4* __restrict__ slots0, const ColliderDev* __restrict__ cols,
-                        const uint32_t* __restrict__ nbr, int32_t* __restrict__ status, int pin0,
-                        int iterations, int last_substep, int with_collide)
+                        const float4* __restrict__ slots0, int32_t* __restrict__ status, int pin0,
+                        int iterations, int last_substep)
 {
     extern __shared__ __align__(128) unsigned char res_smem[];
     ResidentSmem& S = *reinterpret_cast<ResidentSmem*>(res_smem);
@@ -1179,14 +1178,12 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
     const bool stage_lra = ns >= 1 && ns <= kGridLraCached;
 
     // stage the tile and halo (zero outside the cloth; the next buffer's halo starts at
-    // zero and stays so outside the cloth), the rests, the attachments and x.  With the
-    // collision pass folded in, the first buffer starts at zero too and takes the
-    // collision results below.
+    // zero and stays so outside the cloth), the rests, the attachments and x
     if (active) {
         for (int k = tid; k < kResHalo * kResHalo; k += kResThreads) {
             const int ha = k / kResHalo, hb = k - ha * kResHalo;
             const int pa = a0 - 1 + ha, pb = b0 - 1 + hb;
-            const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V && !with_collide;
+            const bool in = pa >= 0 && pa < V && pb >= 0 && pb < V;
             cp_async16_zfill(&S.sp[0][ha][hb], pin + (in ? base + pa * V + pb : base), in);
             S.sp[1][ha][hb] = make_float4(0, 0, 0, 0);
         }
@@ -1207,33 +1204,10 @@ k_grid_substep_resident(const int2* __restrict__ cloth_dom, const DomainParams* 
         ngroups = (ns + gsize - 1) / gsize;
         lra_group_boxes(S.sgl, S.ssup, slots + s0, slots0 + s0, ns, gsize, ngroups, tid);
     }
-    // every block's buffers are cleared before any neighbour stores into them
+    // every block's next buffer is cleared before any neighbour stores into it
     cluster_barrier();
 
-    // the substep's collision pass (k_collide's work for this tile: every particle reads
-    // the positions from before the pass, in global memory), its results into the first
-    // buffer and the neighbours' halos
-    if (with_collide) {
-        if (owns) {
-            const float4 q = collide_particle(D, cols, i, i - D.p_begin, x, pin, nbr, status);
-            const int hx = ta + 1, hy = tb + 1;
-            S.sp[0][hx][hy] = q;
-            const bool up = ta == 0 && rt > 0, down = ta == kResT - 1 && rt < 3;
-            const bool left = tb == 0 && rc > 0, right = tb == kResT - 1 && rc < 3;
-            if (up) st_cluster_f4(&S.sp[0][kResT + 1][hy], (uint32_t)(rank - 4), q);
-            if (down) st_cluster_f4(&S.sp[0][0][hy], (uint32_t)(rank + 4), q);
-            if (left) st_cluster_f4(&S.sp[0][hx][kResT + 1], (uint32_t)(rank - 1), q);
-            if (right) st_cluster_f4(&S.sp[0][hx][0], (uint32_t)(rank + 1), q);
-            if (up && left) st_cluster_f4(&S.sp[0][kResT + 1][kResT + 1], (uint32_t)(rank - 5), q);
-            if (up && right) st_cluster_f4(&S.sp[0][kResT + 1][0], (uint32_t)(rank - 3), q);
-            if (down && left) st_cluster_f4(&S.sp[0][0][kResT + 1], (uint32_t)(rank + 3), q);
-            if (down && right) st_cluster_f4(&S.sp[0][0][0], (uint32_t)(rank + 5), q);
-        }
-        cluster_barrier();  // publishes the halo stores
-    }
-
-    // the iterations' first input is the collision pass's output buffer
-    int pc = with_collide ? pin0 ^ 1 : pin0;
+    int pc = pin0;
     for (int it = 0; it < iterations; ++it) {
         const int cur = it & 1;
         // the previous iteration's halo stores are published by the cluster barrier it
@@ -1593,7 +1567,7 @@ static cudaLaunchConfig_t resident_config(const Launch& L, int n_cloths, cudaLau
 }
 
 cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom, int n_cloths, int pin,
-                                         int iterations, int last_sub, int with_collide)
+                                         int iterations, int last_sub)
 {
     if (n_cloths <= 0 || iterations <= 0) return cudaSuccess;
     const DeviceArrays& d = *L.d;
@@ -1601,8 +1575,7 @@ cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom,
     const cudaLaunchConfig_t cfg = resident_config(L, n_cloths, at);
     return cudaLaunchKernelEx(&cfg, k_grid_substep_resident, cloth_dom, (const DomainParams*)d.dom, d.p[0], d.p[1],
                               d.x, d.v, (const float4*)d.x0, (const float4*)d.grest, (const float4*)d.glra,
-                              (const float4*)d.slots, (const float4*)d.slots0, (const ColliderDev*)d.col,
-                              (const uint32_t*)d.nbr, d.status, pin, iterations, last_sub, with_collide);
+                              (const float4*)d.slots, (const float4*)d.slots0, d.status, pin, iterations, last_sub);
 }
 
 bool substep_resident_supported()

@@ -985,22 +985,21 @@ vt_status World::enqueue_frame(const FrameArgs& a, int32_t ih, bool any_self, cu
             }
             VT_STAGE(ST_CACHE_NEIGHBORS, launch_cache_neighbors(L, pc), "cache_neighbors", pk);
         }
+        VT_STAGE(ST_COLLIDE, launch_collide(L, pc, 1 - pc), "collide", pk);
+        pc = 1 - pc;
         const bool last_sub = sub == a.substeps - 1;
         const int cmode = substep_clusters_mode();
         if (resident_ok_ && a.iterations > 0 && cmode == 1) {
-            // small grid cloths: the collision pass and the substep's iterations in one
-            // launch, positions resident in the clusters' shared memory
+            // small grid cloths: the substep's iterations in one launch, positions resident
+            // in the clusters' shared memory (the collision pass stays k_collide: folded into
+            // this kernel it compiled with other register limits, and the fast build's
+            // contracted arithmetic then differed from a batch's k_collide)
             VT_STAGE(ST_GRID_ITER,
                      launch_grid_substep_resident(L, cloth_doms_dev_, n_resident_cloths_, pc, a.iterations,
-                                                  last_sub ? 1 : 0, 1),
+                                                  last_sub ? 1 : 0),
                      "grid_iter", 1);
-            pc = 1 - pc;  // the collision pass's output buffer
             if (a.iterations % 2) pc = 1 - pc;
-            continue;
-        }
-        VT_STAGE(ST_COLLIDE, launch_collide(L, pc, 1 - pc), "collide", pk);
-        pc = 1 - pc;
-        if (cluster_ok_ && a.iterations > 0 && cmode != 0) {
+        } else if (cluster_ok_ && a.iterations > 0 && cmode != 0) {
             // small grid cloths: the substep's iterations in one launch of clusters
             VT_STAGE(ST_GRID_ITER,
                      launch_grid_substep_cluster(L, cloth_tiles_dev_, n_cluster_cloths_, pc, a.iterations,

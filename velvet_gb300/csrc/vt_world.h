@@ -285,10 +285,8 @@ constexpr int kClusterMaxTiles = 16;
 constexpr int kResidentMaxSide = 64;
 int substep_clusters_mode();
 vt_status set_substep_clusters(int mode);
-// with_collide: the substep's collision pass runs first inside the same launch (pin: the
-// pass's input buffer; the iterations then start from the other one, as after k_collide).
 cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom, int n_cloths, int pin,
-                                         int iterations, int last_sub, int with_collide);
+                                         int iterations, int last_sub);
 bool substep_resident_supported();
 
 cudaError_t launch_presdf_predict(const Launch& L, int pcur);
