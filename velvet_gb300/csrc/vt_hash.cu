@@ -21,7 +21,7 @@
 // equals the order it would have alone.  The solver's walk runs one thread per sorted
 // slot over copies of the positions in sorted order (made with the cell ranges), so a
 // warp's threads share buckets and each candidate is one contiguous 16-byte load (in
-// worlds of up to 131,072 particles a warp per particle, lane per bucket; up to 2,048
+// worlds of up to 49,152 particles a warp per particle, lane per bucket; up to 2,048
 // particles the keys, sort and cell ranges run on one block); the caller-buffer form
 // (HashObjects) walks the caller's float3 arrays directly.
 #include "vt_math.cuh"

@@ -324,9 +324,11 @@ constexpr size_t radix_hist_words(int64_t n)
 cudaError_t launch_cell_ranges(const uint32_t* keys, int32_t n, uint32_t* cell_start,
                                uint32_t* cell_end, cudaStream_t st);
 // The neighbour walk: a warp per particle in worlds of up to kWarpWalkMaxParticles
-// particles (latency-bound: too few particles to hide a thread's serial bucket probes),
-// else a thread per particle (half the instructions).
-constexpr int32_t kWarpWalkMaxParticles = 131072;
+// particles (latency-bound: too few particles to hide a thread's serial chain of probes
+// and candidates), else a thread per particle (half the instructions).  Frame of one
+// cloth, warp / thread form: 64x64 0.241 / 0.342 ms, 128x128 0.355 / 0.446, 181x181
+// 0.419 / 0.475, 256x256 0.576 / 0.559.
+constexpr int32_t kWarpWalkMaxParticles = 49152;
 cudaError_t launch_cache_neighbors(const Launch& L, int pin);
 // Spatial hash of a sparse particle arena (the served form): particles [0, hw) with
 // per-particle domain ids pdom (< 0: free); cells [0, sentinel); n_active live particles.
