@@ -480,8 +480,9 @@ vt_status vt_tuning_set_grid_tile(int32_t variant);
 vt_status vt_tuning_set_tile_loads(int32_t tma);
 /* Small grid cloths run all Jacobi iterations of a substep in one launch of thread-block
  * clusters, one cluster of 16 blocks per cloth, with the cluster's hardware barrier
- * between iterations.  mode 1 (the default): when every cloth of a solver or batch is
- * within 64 x 64 particles, each block keeps one 16 x 16 tile of predicted positions in
+ * between iterations, when the solver's or batch's clusters all fit on the device at once
+ * (else one launch per iteration is faster).  mode 1 (the default): when every cloth of a
+ * solver or batch is within 64 x 64 particles, each block keeps one 16 x 16 tile of predicted positions in
  * shared memory for the whole substep and passes its edges to the neighbouring blocks
  * through distributed shared memory; otherwise, when every cloth is within 16 tiles of
  * the grid kernel, the blocks step through those tiles, reading positions from global

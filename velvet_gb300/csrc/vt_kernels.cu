@@ -22,6 +22,8 @@
 // Also here: read-back packing (k_pack_xyz).  The device grid builder is in vt_build.cu.
 #include <utility>
 
+#include <algorithm>
+
 #include "vt_math.cuh"
 #include "vt_world.h"
 
@@ -1519,13 +1521,14 @@ cudaError_t launch_grid_substep_cluster(const Launch& L, const int2* cloth_tiles
                                     std::make_integer_sequence<int, kGridVariants>{});
 }
 
-// Whether this device runs clusters of kClusterCtas blocks of the substep kernel (a
-// non-portable size: it needs the kernel attribute and a GPC with that many free SMs).
+// How many clusters of kClusterCtas blocks of the substep kernel this device holds at once
+// (0: none; a non-portable size needs the kernel attribute and a GPC with that many free
+// SMs).
 template <int TA, int TB>
-static bool cluster_kernel_fits()
+static int cluster_kernel_capacity()
 {
     auto k = k_grid_substep_cluster<TA, TB>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return false;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 0;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(kClusterCtas);
     cfg.blockDim = dim3(kBlock);
@@ -1537,17 +1540,18 @@ static bool cluster_kernel_fits()
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int n = 0;
-    return cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n >= 1;
+    return cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess ? n : 0;
 }
 
-bool substep_clusters_supported()
+int substep_cluster_capacity()
 {
-    static int ok = -1;
-    if (ok < 0) {
-        ok = cluster_kernel_fits<7, 31>() && cluster_kernel_fits<15, 15>() && cluster_kernel_fits<3, 63>() ? 1 : 0;
+    static int cap = -1;
+    if (cap < 0) {
+        cap = std::min(cluster_kernel_capacity<7, 31>(),
+                       std::min(cluster_kernel_capacity<15, 15>(), cluster_kernel_capacity<3, 63>()));
         (void)cudaGetLastError();  // a refused query leaves no sticky error
     }
-    return ok == 1;
+    return cap;
 }
 
 static cudaLaunchConfig_t resident_config(const Launch& L, int n_cloths, cudaLaunchAttribute* at)
@@ -1578,25 +1582,24 @@ cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom,
                               (const float4*)d.slots, (const float4*)d.slots0, d.status, pin, iterations, last_sub);
 }
 
-bool substep_resident_supported()
+int substep_resident_capacity()
 {
-    static int ok = -1;
-    if (ok < 0) {
+    static int cap = -1;
+    if (cap < 0) {
         auto k = k_grid_substep_resident;
-        bool fits = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
-                    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(ResidentSmem)) == cudaSuccess;
-        if (fits) {
+        int n = 0;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ResidentSmem)) ==
+                cudaSuccess) {
             Launch L{};
             cudaLaunchAttribute at[1];
             const cudaLaunchConfig_t cfg = resident_config(L, 1, at);
-            int n = 0;
-            fits = cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n >= 1;
+            if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) n = 0;
         }
-        ok = fits ? 1 : 0;
+        cap = n;
         (void)cudaGetLastError();  // a refused query leaves no sticky error
     }
-    return ok == 1;
+    return cap;
 }
 
 cudaError_t launch_finalize(const Launch& L, int pcur, int predict_next)

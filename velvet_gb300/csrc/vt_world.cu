@@ -379,7 +379,7 @@ vt_status World::update_cluster_plan()
             }
             doms.push_back(make_int2(gd.first, 0));
         }
-        if (!doms.empty() && substep_resident_supported()) {
+        if (!doms.empty() && (int64_t)doms.size() <= substep_resident_capacity()) {
             VT_CUDA(cudaMemcpy(cloth_doms_dev_, doms.data(), doms.size() * sizeof(int2), cudaMemcpyHostToDevice),
                     "upload resident cloth list");
             n_resident_cloths_ = (int32_t)doms.size();
@@ -395,7 +395,7 @@ vt_status World::update_cluster_plan()
         ranges.push_back(make_int2(t0, t0 + (int32_t)tmp.size()));
         t0 += (int32_t)tmp.size();
     }
-    if (t0 != n_gtiles || !substep_clusters_supported()) return VT_OK;
+    if (t0 != n_gtiles || (int64_t)ranges.size() > substep_cluster_capacity()) return VT_OK;
     VT_CUDA(cudaMemcpy(cloth_tiles_dev_, ranges.data(), ranges.size() * sizeof(int2), cudaMemcpyHostToDevice),
             "upload cloth tile ranges");
     n_cluster_cloths_ = (int32_t)ranges.size();

@@ -271,7 +271,12 @@ cudaError_t prepare_kernels();
 // cluster per cloth, cloth_tiles[c] its tile range); see k_grid_substep_cluster.
 cudaError_t launch_grid_substep_cluster(const Launch& L, const int2* cloth_tiles, int n_cloths, int pin,
                                         int iterations, int last_sub);
-bool substep_clusters_supported();
+// Clusters of the substep kernels this device holds at once (0: none).  A world takes a
+// cluster form only when one cluster per cloth fits at once: with more cloths the clusters
+// run in waves, each paying a substep's whole chain of iterations, and one launch per
+// iteration is faster (a batch of 32 cloths of sides 24-48: 0.45 ms per frame per
+// iteration, 0.68 resident, 0.83 re-staging).
+int substep_cluster_capacity();
 // Grid cloths of at most this many tiles (of the variant in use) take the cluster kernel:
 // one tile per block, a single round per iteration.  (With two rounds — a 64x64 cloth's 25
 // tiles of 15x15 on 16 blocks — each iteration pays the tile's dependent-latency chain
@@ -287,7 +292,7 @@ int substep_clusters_mode();
 vt_status set_substep_clusters(int mode);
 cudaError_t launch_grid_substep_resident(const Launch& L, const int2* cloth_dom, int n_cloths, int pin,
                                          int iterations, int last_sub);
-bool substep_resident_supported();
+int substep_resident_capacity();
 
 cudaError_t launch_presdf_predict(const Launch& L, int pcur);
 cudaError_t launch_collide(const Launch& L, int pin, int pout);
