@@ -78,6 +78,43 @@ def test_batch_of_tiny_cloths_matches_the_oracle():
         o.close()
 
 
+def test_batch_of_more_small_cloths_than_clusters_fit_equals_each_alone():
+    """64 cloths of 8-24 particles a side: more 16-block clusters than the device holds at
+    once, so the batch runs one launch per Jacobi iteration while each cloth alone runs the
+    cluster-resident substep — the same bits either way, and the batch's frame launches
+    the tile kernel once per iteration."""
+    import ctypes as C
+
+    wl = W.batched(64, frames=3, seed=8, lo=8, hi=24)
+    batch = vg.BatchSolver()
+    alone = []
+    for spec in wl.cloths:
+        s = vg.ClothSolver()
+        W.build_plain(spec, s)
+        batch.add(s)
+        s.close()
+        o = vg.ClothSolver()
+        W.build_plain(spec, o)
+        alone.append((o, spec))
+    for f in range(wl.frames):
+        n0 = C.c_uint64()
+        assert vg.lib().vt_batch_launch_count(batch.handle, C.byref(n0)) == 0
+        batch.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin)
+        n1 = C.c_uint64()
+        assert vg.lib().vt_batch_launch_count(batch.handle, C.byref(n1)) == 0
+        for o, spec in alone:
+            o.simulate(wl.frame_dt, wl.substeps, wl.iterations, wl.relaxation, wl.friction,
+                       wl.collision_margin, spec.particle_diameter())
+    assert n1.value - n0.value >= wl.substeps * wl.iterations, "one launch per iteration"
+    batch.sync()
+    for k, (o, spec) in enumerate(alone):
+        o.sync()
+        assert np.array_equal(bits(batch.positions(k)), bits(o.positions())), f"cloth {k} positions"
+        assert np.array_equal(bits(batch.velocities(k)), bits(o.velocities())), f"cloth {k} velocities"
+        o.close()
+
+
 def test_batch_mixing_kernel_kinds_equals_each_cloth_alone():
     """One batch holding grid cloths on the tile kernel, grid cloths on the CSR kernels
     (vt_solver_use_grid_kernel off) and a cloth whose 24 LRA slots take the slot-group
