@@ -372,13 +372,13 @@ __device__ __forceinline__ void bend_eval(float4 a0, float4 a1, float4 a2, float
 // endpoint may evaluate it.
 __device__ __forceinline__ bool stretch_common(float4 pa, float4 pb, float rest, vec3& common)
 {
-    const vec3 diff = xyz(pa) - xyz(pb);
+    const vec3 diff = sub_p(xyz(pa), xyz(pb));
     const float d = length_exact(diff);
     const float denom = pa.w + pb.w;
     if (!(d != rest && denom > 0)) return false;
     const vec3 grad = diff / (d + VT_EPSILON);
     const float lambda = (d - rest) / denom;
-    common = grad * lambda;
+    common = mul_p(grad, lambda);
     return true;
 }
 
@@ -540,7 +540,7 @@ __device__ __forceinline__ vec3 jacobi_apply(const DomainParams& D, vec3 pi, vec
 {
     if (cnt > 0) {
         const float count = (float)cnt;
-        pi = pi + (acc / count) * D.relax;
+        pi = madd_p(acc / count, D.relax, pi);
     }
     return pi;
 }
@@ -686,7 +686,7 @@ __device__ __forceinline__ bool stretch_common_d(vec3 diff, float d, float wa, f
     if (!(d != rest && denom > 0)) return false;
     const vec3 grad = diff / (d + VT_EPSILON);
     const float lambda = (d - rest) / denom;
-    common = grad * lambda;
+    common = mul_p(grad, lambda);
     return true;
 }
 
@@ -704,19 +704,20 @@ __device__ __forceinline__ void bend_eval_grid(float4 a0, float4 a1, float4 a2, 
     c1 = c0;
     c2 = c0;
     c3 = c0;
-    const vec3 e = p3 - p2;
+    const vec3 e = sub_p(p3, p2);
     const float elen = d3;
     if (elen < VT_EPSILON) return;
     const float inv = 1.0f / elen;
     // the angle chain in exact operations (vt_math.cuh: acos near a flat pair)
-    vec3 n1 = cross_exact(p2 - p0, p3 - p0);
+    const vec3 p20 = sub_p(p2, p0), p21 = sub_p(p2, p1);
+    vec3 n1 = cross_exact(p20, sub_p(p3, p0));
     n1 = div_exact(n1, dot_exact(n1, n1));
-    vec3 n2 = cross_exact(p3 - p1, p2 - p1);
+    vec3 n2 = cross_exact(sub_p(p3, p1), p21);
     n2 = div_exact(n2, dot_exact(n2, n2));
-    const vec3 d0 = n1 * elen;
-    const vec3 d1 = n2 * elen;
-    const vec3 d2 = n1 * (dot(p0 - p3, e) * inv) + n2 * (dot(p1 - p3, e) * inv);
-    const vec3 dd3 = n1 * (dot(p2 - p0, e) * inv) + n2 * (dot(p2 - p1, e) * inv);
+    const vec3 d0 = mul_p(n1, elen);
+    const vec3 d1 = mul_p(n2, elen);
+    const vec3 d2 = madd_p(n2, dot(sub_p(p1, p3), e) * inv, mul_p(n1, dot(sub_p(p0, p3), e) * inv));
+    const vec3 dd3 = madd_p(n2, dot(p21, e) * inv, mul_p(n1, dot(p20, e) * inv));
     n1 = normalize_exact(n1);
     n2 = normalize_exact(n2);
     const float phi = vt_acosf_exact(gclamp(dot_exact(n1, n2), -1.0f, 1.0f));
@@ -726,8 +727,8 @@ __device__ __forceinline__ void bend_eval_grid(float4 a0, float4 a1, float4 a2, 
     if (lambda < VT_EPSILON) return;
     lambda = (phi - rest) / (lambda + xpbd);
     if (dot_exact(cross_exact(n1, n2), e) > 0.0f) lambda = -lambda;
-    const vec3 k0 = d0 * (-w0 * lambda), k1 = d1 * (-w1 * lambda);
-    const vec3 k2 = d2 * (-w2 * lambda), k3 = dd3 * (-w3 * lambda);
+    const vec3 k0 = mul_p(d0, -w0 * lambda), k1 = mul_p(d1, -w1 * lambda);
+    const vec3 k2 = mul_p(d2, -w2 * lambda), k3 = mul_p(dd3, -w3 * lambda);
     c0 = make_float4(k0.x, k0.y, k0.z, 1.0f);
     c1 = make_float4(k1.x, k1.y, k1.z, 1.0f);
     c2 = make_float4(k2.x, k2.y, k2.z, 1.0f);
@@ -803,7 +804,7 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
 #define VT_TAKE(s4, scale)                              \
     do {                                                \
         const float4 s_ = (s4);                         \
-        acc3(acc, mk3(s_.x, s_.y, s_.z) * (scale));     \
+        acc = madd_p(xyz(s_), (scale), acc);            \
         cnt += s_.w != 0.0f ? 1 : 0;                    \
     } while (0)
     // stretch, constraint order: generators (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
@@ -847,7 +848,7 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
 #define VT_CORNER(c4)                       \
     do {                                    \
         const float4 c_ = (c4);             \
-        acc3(acc, xyz(c_));                 \
+        acc3_p(acc, xyz(c_));               \
         cnt += c_.w != 0.0f ? 1 : 0;        \
     } while (0)
     VT_CORNER(sbd[1][gx - 1][gy - 1]);

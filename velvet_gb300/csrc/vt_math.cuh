@@ -25,6 +25,12 @@
 #else
 #define VT_FAST_DEVICE 0
 #endif
+// device code for sm_100 and later: paired FP32 arithmetic (sub_p, mul_p, ... below)
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+#define VT_PAIRED 1
+#else
+#define VT_PAIRED 0
+#endif
 
 struct vec3 {
     float x, y, z;
@@ -38,7 +44,11 @@ VT_HD vec3 operator-(vec3 a) { return mk3(-a.x, -a.y, -a.z); }
 VT_HD vec3 operator*(vec3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
 VT_HD vec3 operator/(vec3 a, float s)
 {
-#if VT_FAST_DEVICE
+#if VT_FAST_DEVICE && VT_PAIRED
+    const float r = 1.0f / s;
+    const float2 q = __fmul2_rn(make_float2(a.x, a.y), make_float2(r, r));
+    return mk3(q.x, q.y, a.z * r);
+#elif VT_FAST_DEVICE
     const float r = 1.0f / s;
     return mk3(a.x * r, a.y * r, a.z * r);
 #else
@@ -65,7 +75,11 @@ VT_HD vec3 normalize(vec3 a)
 // corrections themselves use the fast arithmetic.
 VT_HD float dot_exact(vec3 a, vec3 b)
 {
-#if VT_FAST_DEVICE
+#if VT_PAIRED
+    // the x and y products as one paired multiply, rounded as two
+    const float2 xy = __fmul2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y));
+    return __fadd_rn(__fadd_rn(xy.x, xy.y), __fmul_rn(a.z, b.z));
+#elif VT_FAST_DEVICE
     return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
 #else
     return dot(a, b);
@@ -126,6 +140,57 @@ VT_HD void acc3(vec3& a, vec3 b)
     a.x = a.x + b.x;
     a.y = a.y + b.y;
     a.z = a.z + b.z;
+}
+
+// Paired FP32 arithmetic.  sm_100 and later issue the x and y halves of a vector add,
+// multiply or fused multiply-add as one instruction (__fadd2_rn, __fmul2_rn, __ffma2_rn),
+// each half rounded as the scalar operation is, so a paired form has its scalar form's
+// bits.  The hot vector operations of the Jacobi iteration use these forms; host code
+// takes the scalar ones.  Where the scalar form is a product followed by a sum, the fast
+// build fuses them (__ffma2_rn), as its contraction would; the exact build must round
+// both, and a paired product feeding a paired sum is fused into one paired FMA by the
+// code generator even without contraction (-fmad=false) and with the PTX .rn forms
+// (measured on sm_103a: 43% of uniform random operands differ from the two roundings),
+// so its paired product is followed by scalar sums (__fadd_rn, never fused), which keeps
+// the bits on every operand tested.
+VT_HD vec3 sub_p(vec3 a, vec3 b)  // a - b
+{
+#if VT_PAIRED
+    const float2 r = __fadd2_rn(make_float2(a.x, a.y), make_float2(-b.x, -b.y));
+    return mk3(r.x, r.y, a.z - b.z);
+#else
+    return a - b;
+#endif
+}
+VT_HD vec3 mul_p(vec3 a, float s)  // a * s
+{
+#if VT_PAIRED
+    const float2 r = __fmul2_rn(make_float2(a.x, a.y), make_float2(s, s));
+    return mk3(r.x, r.y, a.z * s);
+#else
+    return a * s;
+#endif
+}
+VT_HD vec3 madd_p(vec3 a, float s, vec3 b)  // a * s + b
+{
+#if VT_PAIRED && VT_FAST_DEVICE
+    const float2 r = __ffma2_rn(make_float2(a.x, a.y), make_float2(s, s), make_float2(b.x, b.y));
+    return mk3(r.x, r.y, __fmaf_rn(a.z, s, b.z));
+#elif VT_PAIRED
+    const float2 p = __fmul2_rn(make_float2(a.x, a.y), make_float2(s, s));
+    return mk3(__fadd_rn(p.x, b.x), __fadd_rn(p.y, b.y), __fadd_rn(__fmul_rn(a.z, s), b.z));
+#else
+    return a * s + b;
+#endif
+}
+VT_HD void acc3_p(vec3& acc, vec3 b)  // acc += b
+{
+#if VT_PAIRED
+    const float2 r = __fadd2_rn(make_float2(acc.x, acc.y), make_float2(b.x, b.y));
+    acc = mk3(r.x, r.y, acc.z + b.z);
+#else
+    acc3(acc, b);
+#endif
 }
 
 // mat4 (column-major) * (v, w), glm association
