@@ -781,6 +781,50 @@ __device__ __forceinline__ void grid_generator(int X, int Y, int R, const float4
     sbd[3][gx][gy] = c3;
 }
 
+// A stored constraint term s (its correction in xyz, 1 in w when it fired) taken into the
+// particle's sums.  Fast build: (x, y) += s.xy * scale and (z, count) += (s.z * scale,
+// s.w), two paired FMAs (sm_100 and later), the count summed in FP32 beside z (exact for
+// counts this small).  Exact build: (x, y) by a paired product and scalar sums (a paired
+// product feeding a paired sum would be fused by the code generator), z by a scalar
+// product and sum, and the flag into the integer count — carrying the count in the
+// paired sums (with the corners' below) ran slower there (mix 1.552e10 -> 1.538e10
+// pit/s), while it took the fast build from 1.806e10 to 1.820e10.
+__device__ __forceinline__ void take_term(float2& axy, float2& azc, int& cnt, float4 s, float scale)
+{
+#if VT_PAIRED && VT_FAST_DEVICE
+    axy = __ffma2_rn(make_float2(s.x, s.y), make_float2(scale, scale), axy);
+    azc = __ffma2_rn(make_float2(s.z, s.w), make_float2(scale, 1.0f), azc);
+#elif VT_PAIRED
+    const float2 p = __fmul2_rn(make_float2(s.x, s.y), make_float2(scale, scale));
+    axy = make_float2(__fadd_rn(axy.x, p.x), __fadd_rn(axy.y, p.y));
+    azc.x = __fadd_rn(azc.x, __fmul_rn(s.z, scale));
+    cnt += s.w != 0.0f ? 1 : 0;
+#else
+    axy = make_float2(axy.x + s.x * scale, axy.y + s.y * scale);
+    azc.x = azc.x + s.z * scale;
+    cnt += s.w != 0.0f ? 1 : 0;
+#endif
+}
+// A bending corner c (its correction in xyz, 1 in w when it fired): (x, y) += c.xy and,
+// in the fast build, (z, count) += c.zw as one paired sum; the exact build adds z alone
+// and the flag to the integer count (the paired form ran slower there, mix 1.558e10 ->
+// 1.541e10 pit/s).
+__device__ __forceinline__ void take_corner(float2& axy, float2& azc, int& cnt, float4 c)
+{
+#if VT_PAIRED && VT_FAST_DEVICE
+    axy = __fadd2_rn(axy, make_float2(c.x, c.y));
+    azc = __fadd2_rn(azc, make_float2(c.z, c.w));
+#elif VT_PAIRED
+    axy = __fadd2_rn(axy, make_float2(c.x, c.y));
+    azc.x = __fadd_rn(azc.x, c.z);
+    cnt += c.w != 0.0f ? 1 : 0;
+#else
+    axy = make_float2(axy.x + c.x, axy.y + c.y);
+    azc.x = azc.x + c.z;
+    cnt += c.w != 0.0f ? 1 : 0;
+#endif
+}
+
 // The Jacobi sum of grid particle (a, b), i = its index: its eight stretch constraints,
 // its LRA attachments in slot order, its four bending corners, all in constraint order.
 // Generator (a, b)'s results sit at [gx][gy] of sst / sbd, generator (a-1, b-1)'s at
@@ -800,23 +844,20 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
     const float nw = -wi;
     // Branch-free: a constraint that does not exist (outside the cloth) or did not fire is
     // stored as all zeros, so its term adds +-0, which leaves the sum's bits unchanged (the
-    // sum starts at +0 and an exact IEEE sum is never -0), and the count takes the flag.
-#define VT_TAKE(s4, scale)                              \
-    do {                                                \
-        const float4 s_ = (s4);                         \
-        acc = madd_p(xyz(s_), (scale), acc);            \
-        cnt += s_.w != 0.0f ? 1 : 0;                    \
-    } while (0)
+    // sum starts at +0 and an exact IEEE sum is never -0).  Its w (1 when it fired, else 0)
+    // is summed in FP32 beside z, so a term is two paired operations on (x, y) and
+    // (z, count); counts this small are exact in FP32.
+    float2 axy = make_float2(acc.x, acc.y), azc = make_float2(acc.z, 0.0f);
     // stretch, constraint order: generators (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b)
-    VT_TAKE(sst[2][gx - 1][gy - 1], wi);  // t2, second endpoint
-    VT_TAKE(sst[1][gx - 1][gy], wi);      // t1, second endpoint
-    VT_TAKE(sst[3][gx - 1][gy], wi);      // t3, second endpoint
-    VT_TAKE(sst[0][gx][gy - 1], wi);      // t0, second endpoint
-    VT_TAKE(sst[3][gx][gy - 1], nw);      // t3, first endpoint
-    VT_TAKE(sst[0][gx][gy], nw);          // t0, first endpoint
-    VT_TAKE(sst[1][gx][gy], nw);          // t1, first endpoint
-    VT_TAKE(sst[2][gx][gy], nw);          // t2, first endpoint
-#undef VT_TAKE
+    take_term(axy, azc, cnt, sst[2][gx - 1][gy - 1], wi);  // t2, second endpoint
+    take_term(axy, azc, cnt, sst[1][gx - 1][gy], wi);      // t1, second endpoint
+    take_term(axy, azc, cnt, sst[3][gx - 1][gy], wi);      // t3, second endpoint
+    take_term(axy, azc, cnt, sst[0][gx][gy - 1], wi);      // t0, second endpoint
+    take_term(axy, azc, cnt, sst[3][gx][gy - 1], nw);      // t3, first endpoint
+    take_term(axy, azc, cnt, sst[0][gx][gy], nw);          // t0, first endpoint
+    take_term(axy, azc, cnt, sst[1][gx][gy], nw);          // t1, first endpoint
+    take_term(axy, azc, cnt, sst[2][gx][gy], nw);          // t2, first endpoint
+    acc = mk3(axy.x, axy.y, azc.x);
     // long-range attachments, slot order; pairs that cannot fire skip their square roots
     if (ns) {
         if (ns <= kGridLraCached) {
@@ -845,17 +886,14 @@ __device__ __forceinline__ void grid_particle_sum(int a, int b, int R, int i, in
     }
     // bending corners, constraint order: quads (a-1,b-1) < (a-1,b) < (a,b-1) < (a,b);
     // branch-free as the stretch terms above
-#define VT_CORNER(c4)                       \
-    do {                                    \
-        const float4 c_ = (c4);             \
-        acc3_p(acc, xyz(c_));               \
-        cnt += c_.w != 0.0f ? 1 : 0;        \
-    } while (0)
-    VT_CORNER(sbd[1][gx - 1][gy - 1]);
-    VT_CORNER(sbd[3][gx - 1][gy]);
-    VT_CORNER(sbd[2][gx][gy - 1]);
-    VT_CORNER(sbd[0][gx][gy]);
-#undef VT_CORNER
+    axy = make_float2(acc.x, acc.y);
+    azc.x = acc.z;
+    take_corner(axy, azc, cnt, sbd[1][gx - 1][gy - 1]);
+    take_corner(axy, azc, cnt, sbd[3][gx - 1][gy]);
+    take_corner(axy, azc, cnt, sbd[2][gx][gy - 1]);
+    take_corner(axy, azc, cnt, sbd[0][gx][gy]);
+    acc = mk3(axy.x, axy.y, azc.x);
+    cnt += (int)azc.y;
 }
 
 // The tile kernel: a block owns a TA x TB tile; it stages the tile and a one-particle
