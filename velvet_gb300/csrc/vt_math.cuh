@@ -25,7 +25,7 @@
 #else
 #define VT_FAST_DEVICE 0
 #endif
-// device code for sm_100 and later: paired FP32 arithmetic (sub_p, mul_p, ... below)
+// device code for sm_100 and later: paired FP32 arithmetic (sub_p, mul_p, madd_p below)
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
 #define VT_PAIRED 1
 #else
@@ -181,15 +181,6 @@ VT_HD vec3 madd_p(vec3 a, float s, vec3 b)  // a * s + b
     return mk3(__fadd_rn(p.x, b.x), __fadd_rn(p.y, b.y), __fadd_rn(__fmul_rn(a.z, s), b.z));
 #else
     return a * s + b;
-#endif
-}
-VT_HD void acc3_p(vec3& acc, vec3 b)  // acc += b
-{
-#if VT_PAIRED
-    const float2 r = __fadd2_rn(make_float2(acc.x, acc.y), make_float2(b.x, b.y));
-    acc = mk3(r.x, r.y, acc.z + b.z);
-#else
-    acc3(acc, b);
 #endif
 }
 
