@@ -365,6 +365,20 @@ __device__ __forceinline__ void bend_eval(float4 a0, float4 a1, float4 a2, float
     c3 = make_float4(k3.x, k3.y, k3.z, 1.0f);
 }
 
+// lambda * gradient of a distance constraint that fires: (diff / (d + eps)) * ((d - rest)
+// / denom), the reference's two divisions (VtClothSolverGPU.cu:87-91).  The fast build
+// takes one: diff * ((d - rest) / (denom * (d + eps))), within its tolerance.
+__device__ __forceinline__ vec3 stretch_scale(vec3 diff, float d, float denom, float rest)
+{
+#if VT_FAST_DEVICE
+    return mul_p(diff, (d - rest) / (denom * (d + VT_EPSILON)));
+#else
+    const vec3 grad = diff / (d + VT_EPSILON);
+    const float lambda = (d - rest) / denom;
+    return mul_p(grad, lambda);
+#endif
+}
+
 // One distance constraint, SolveStretch_Kernel (VtClothSolverGPU.cu:76-98): returns
 // whether it fires and `common` = lambda * gradient, gradient taken from pa - pb.  The
 // reference adds -w_a * common to a and w_b * common to b.  Evaluated from the other
@@ -376,9 +390,7 @@ __device__ __forceinline__ bool stretch_common(float4 pa, float4 pb, float rest,
     const float d = length_exact(diff);
     const float denom = pa.w + pb.w;
     if (!(d != rest && denom > 0)) return false;
-    const vec3 grad = diff / (d + VT_EPSILON);
-    const float lambda = (d - rest) / denom;
-    common = mul_p(grad, lambda);
+    common = stretch_scale(diff, d, denom, rest);
     return true;
 }
 
@@ -684,9 +696,7 @@ __device__ __forceinline__ bool stretch_common_d(vec3 diff, float d, float wa, f
 {
     const float denom = wa + wb;
     if (!(d != rest && denom > 0)) return false;
-    const vec3 grad = diff / (d + VT_EPSILON);
-    const float lambda = (d - rest) / denom;
-    common = mul_p(grad, lambda);
+    common = stretch_scale(diff, d, denom, rest);
     return true;
 }
 
