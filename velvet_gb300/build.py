@@ -15,14 +15,15 @@ checked: -DVT_CHECKED=1 range-checks data-dependent device indices; a failure is
 by the sync calls (the library the tests can load instead with VT_CHECKED=1).
 fast: the solver kernels are compiled as nvcc compiles by default (-fmad=true, so a
 multiply followed by an add may become one FMA, as in the reference's own build) plus
-approximate division and square root, with CUDA's acosf for the dihedral angle and
-reciprocals taken once per vector division (-DVT_FAST=1).  Results differ from the exact
+approximate division and square root, with reciprocals taken once per vector division
+and one division per distance correction (-DVT_FAST=1).  Results differ from the exact
 build in the last bits of each operation; the tests bound the difference by the
 solver's stated tolerance.  The spatial hash (vt_hash.cu), its allocation-free entry
 point and the device grid builder (vt_build.cu) keep the exact flags, so cell keys, sort
 order and neighbour lists of given positions, and a cloth built on the device, are
-bit-identical in every variant; threshold decisions inside the fast kernels use exact
-distances too (vt_math.cuh).  Host code keeps -ffp-contract=off.
+bit-identical in every variant; threshold decisions and the bending-angle chain inside
+the fast kernels use exact operations too (vt_math.cuh).  Host code keeps
+-ffp-contract=off.
 """
 from __future__ import annotations
 

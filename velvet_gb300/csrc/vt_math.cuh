@@ -8,10 +8,11 @@
 // The exact build compiles the translation units that include this file with
 // -fmad=false, so no multiply-add pair is contracted into an FMA: every result is the
 // IEEE-rounded value of the operations as written, on the device and in host code alike.
-// The fast build (VT_FAST, device code only) divides a vector by one reciprocal, takes
-// normalize's reciprocal square root in one step and calls CUDA's acosf; with its
-// compiler flags (contraction, approximate division and square root) its results are
-// within the solver's stated tolerance of the exact ones, not equal to them.
+// The fast build (VT_FAST, device code only) divides a vector by one reciprocal and takes
+// normalize's reciprocal square root in one step; with its compiler flags (contraction,
+// approximate division and square root) its results are within the solver's stated
+// tolerance of the exact ones, not equal to them.  Its threshold distances and its
+// bending-angle chain keep the exact build's operations (dot_exact ... vt_acosf_exact).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -242,9 +243,6 @@ VT_HD float vt_asin_series(float t)
 
 VT_HD float vt_acosf(float x)
 {
-#if VT_FAST_DEVICE
-    return acosf(x);
-#else
     const float pio2_hi = 1.57079637050628662109375f;
     const float pio2_lo = -4.37113900018624283e-8f;
     if (x >= 0.5f) {
@@ -256,7 +254,6 @@ VT_HD float vt_acosf(float x)
         return ((pio2_hi - vt_asin_series(s)) + pio2_lo) * 2.0f;
     }
     return (pio2_hi - vt_asin_series(x)) + pio2_lo;
-#endif
 }
 
 // vt_acosf with every operation rounded as written (the fast build's exact angle chain).
